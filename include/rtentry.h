@@ -1,0 +1,193 @@
+/*
+ * rtentry.h -- C ABI of rt_entry_gb300, a GB300 (sm_103a) implementation of
+ * rt_entry's query path: PCA projection, kd-tree leaf point location (the
+ * entry points) and proximity-graph beam search.
+ *
+ * The reference has no library API; its boundary is the `Graph` class
+ * (graph.h:10-82) driven from main.cpp:82-92.  Each entry point below names
+ * the reference method it replaces.  Conventions:
+ *   - No function exits the process; every failure returns a status and sets
+ *     a thread-local message readable with rte_last_error().
+ *   - Pointers to vectors/ids may be host or device memory (detected per
+ *     call); results are written to the same kind of memory they point to.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  A call that
+ *     reads or writes host memory returns after its results are in place.
+ *   - An index is single-writer: build/load/free must not overlap other calls
+ *     on the same index.  Searches on distinct streams may run concurrently.
+ *   - Data contract (graph.h, file_read.cu): FP32 row-major vectors, int32
+ *     graph [np x degree] with a power-of-two degree and padding value np,
+ *     ids in [0, np], np < 2^31.
+ */
+#ifndef RTENTRY_H_
+#define RTENTRY_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RTE_ABI_VERSION 1
+
+typedef struct rte_index rte_index;
+
+typedef enum {
+  RTE_OK = 0,
+  RTE_EINVAL = 1,   /* bad argument (reference: undefined behaviour or exit) */
+  RTE_ENOMEM = 2,   /* host or device allocation failed                      */
+  RTE_EIO = 3,      /* file missing, truncated or malformed (file_read.cu exit(1)) */
+  RTE_ECUDA = 4,    /* a CUDA call failed (helper.h CUDA_CHECK exit(2))       */
+  RTE_ETIMEOUT = 5, /* a bounded device wait ran out                          */
+  RTE_ESTATE = 6    /* a required build step has not run yet                  */
+} rte_status;
+
+typedef enum { RTE_PREC_FP32 = 0, RTE_PREC_BF16 = 1, RTE_PREC_FP8 = 2 } rte_precision;
+
+typedef enum {
+  RTE_ENTRY_RANDOM = 0, /* LCG entries per query, ALGO 0/2 (graph_search.cuh:50-54,485) */
+  RTE_ENTRY_KDTREE = 1, /* kd-tree leaf of the projected query, ALGO 1 (entry.cu:100-149) */
+  RTE_ENTRY_LEARNED = 2 /* MLP-proposed leaf (no reference counterpart)                 */
+} rte_entry_mode;
+
+/* Search parameters (flags.cpp:3-101 + graph_search.cuh:4-5 macros). */
+typedef struct {
+  int k;             /* topk returned per query; 0 -> beam (graph.cu:54)              */
+  int beam;          /* n_candidates L; rounded up to a power of two (graph.cu:53)    */
+  int search_width;  /* W: nodes expanded per iteration (FLAGS_search_width)          */
+  int max_iter;      /* FLAGS_max_iter, default 100                                   */
+  int bloom_words;   /* visited-set filter size in 32-bit words (SIZE, default 512)   */
+  int bloom_hashes;  /* hash functions (num_hash, default 3)                          */
+  int precision;     /* rte_precision of candidate distances                          */
+  int rerank;        /* 1: exact FP32 rerank of the final beam (graph_helper.cu:146)  */
+  int entry_mode;    /* rte_entry_mode                                                */
+  int warps_per_block; /* 0 = automatic                                                */
+} rte_search_params;
+
+typedef struct {
+  int64_t np;          /* base vectors                                   */
+  int dim;             /* input dimension                                */
+  int search_dim;      /* dimension searched (PCA keep_dims or dim)      */
+  int degree;          /* graph degree                                   */
+  int has_pca;
+  int has_kdtree;
+  int64_t n_leaves;
+  int leaf_size;       /* max points per leaf (max_node)                 */
+  float expand_ratio;
+  int has_bf16;
+  int has_fp8;
+  int device;
+  int64_t device_bytes; /* device memory held by the index               */
+} rte_index_info;
+
+/* Default parameters: k=10, beam=64, W=1, max_iter=100, 512 words, 3 hashes,
+ * FP32, no rerank, kd-tree entries. */
+void rte_default_params(rte_search_params* p);
+
+/* Build an index from host or device arrays (Graph::Input + Graph::RB_Graph,
+ * graph.cu:73-139).  base [np x dim] FP32, graph [np x degree] int32.  The
+ * graph is validated (ids in [0, np], power-of-two degree). */
+rte_status rte_index_from_host(const float* base, int64_t np, int dim, const int32_t* graph,
+                               int degree, int device, rte_index** out);
+
+/* Load base vectors (.fvecs / .fbin / .bvecs, file_read.cu:16-80) and a raw
+ * int32 graph whose degree is file size / (4 np) (file_read.cu:237-255). */
+rte_status rte_index_load(const char* base_path, const char* graph_path, int device,
+                          rte_index** out);
+
+/* PCA of the base (Graph::Projection, graph.cu:141-252; pca.cpp:4-58,122-126):
+ * FP64 mean and covariance, FP64 eigendecomposition, eigenvectors sorted by
+ * descending eigenvalue; the base is projected onto the first keep_dims
+ * components ((B - mean) V) and searched in that space.  keep_dims in
+ * [3, dim]; 0 -> dim. */
+rte_status rte_build_pca(rte_index* idx, int keep_dims);
+
+/* Install a PCA computed elsewhere (mean [dim], rotation [dim x dim], row =
+ * input dim, column = component -- the layout of O.fbin, pca.cpp:78-87) and
+ * project the base with it. */
+rte_status rte_set_pca(rte_index* idx, const float* mean, const float* rotation, int keep_dims);
+
+/* kd-tree over the first three search-space coordinates with at most
+ * leaf_size points per leaf, then boxes enlarged by expand_ratio * width per
+ * side (RT_Entry::BlockUp, entry.cu:8-77; kdtree.cpp:140-196; aabb.cu:27-38).
+ * The reference's point_ratio maps to leaf_size = (int)(np * point_ratio). */
+rte_status rte_build_kdtree(rte_index* idx, int leaf_size, float expand_ratio);
+
+/* Query projection (Graph::Search step 1, graph.cu:258-273): out[nq x
+ * search_dim] = (Q - mean) V[:, :search_dim]. */
+rte_status rte_project(rte_index* idx, const float* queries, int64_t nq, float* out,
+                       void* stream);
+
+/* Entry stage alone (RT_Entry::Search, entry.cu:100-149; devicePrograms.cu:
+ * 29-96): out_leaf[q] = smallest leaf whose expanded box contains the first
+ * three coordinates of projected[q] (row stride search_dim), 0 if none. */
+rte_status rte_locate(rte_index* idx, const float* projected, int64_t nq, int32_t* out_leaf,
+                      void* stream);
+
+/* The whole query path (Graph::Search, graph.cu:254-293): projection, entry
+ * selection, beam search (GraphSearchKernel, graph_search.cuh:56-1964).
+ * out_ids [nq x k] (|pool id|, np for an empty slot), out_dists [nq x k]
+ * squared L2 in the search space (536870912.0f for an empty slot) or NULL. */
+rte_status rte_search(rte_index* idx, const float* queries, int64_t nq,
+                      const rte_search_params* params, int32_t* out_ids, float* out_dists,
+                      void* stream);
+
+/* Beam search from already projected queries [nq x search_dim].  hits [nq]
+ * gives each query's leaf (NULL: run rte_locate first).  Used to feed
+ * identical inputs to the search and to its checker. */
+rte_status rte_search_projected(rte_index* idx, const float* projected, const int32_t* hits,
+                                int64_t nq, const rte_search_params* params, int32_t* out_ids,
+                                float* out_dists, void* stream);
+
+/* Per-query work counters of the last rte_search_projected-equivalent run:
+ * [nq x 4] int64 = valid entries, expanded nodes, distance evaluations,
+ * iterations.  Runs the search once more with counting enabled. */
+rte_status rte_search_counters(rte_index* idx, const float* projected, const int32_t* hits,
+                               int64_t nq, const rte_search_params* params, int64_t* counters,
+                               void* stream);
+
+rte_status rte_index_get_info(const rte_index* idx, rte_index_info* info);
+
+/* Copies of built artifacts (host pointers): mean [dim], rotation
+ * [dim x dim], eigenvalues [dim] (descending, FP64). */
+rte_status rte_get_pca(const rte_index* idx, float* mean, float* rotation, double* eigvals);
+/* Search-space base vectors, row-major [np x search_dim]. */
+rte_status rte_get_search_base(const rte_index* idx, float* out);
+/* The search-space base as a reduced-precision search sees it, widened to
+ * FP32, row-major [np x search_dim]: precision 1 = BF16 values, 2 = FP8-E4M3
+ * values times their per-vector scale (scale = max|x| / 448). */
+rte_status rte_get_search_base_lowp(const rte_index* idx, int precision, float* out);
+/* Leaves in DFS order: tight [n_leaves x 6], expanded [n_leaves x 6]
+ * (minX,minY,minZ,maxX,maxY,maxZ), pids [n_leaves x leaf_size] padded np.
+ * Any pointer may be NULL. */
+rte_status rte_get_kdtree(const rte_index* idx, float* tight, float* expanded, int32_t* pids);
+
+/* Save / load every built artifact to / from a directory (base.fbin,
+ * graph.ibin, mean.fbin, O.fbin, pca_base.fbin and the leaf cache
+ * <leaf_size>_0.aabbs in the reference's layouts, entry.cu:171-190). */
+rte_status rte_index_save(const rte_index* idx, const char* dir);
+rte_status rte_index_load_dir(const char* dir, int device, rte_index** out);
+
+void rte_index_free(rte_index* idx);
+
+/* Host build steps on their own (no device, no index): the kd-tree leaves
+ * of rte_build_kdtree (kdtree.cpp:140-196 + aabb.cu:27-38) over xyz [n x 3],
+ * written to caller arrays of capacity max_leaves (tight / expanded
+ * [max_leaves x 6], pids [max_leaves x leaf_size]); *n_leaves receives the
+ * count (RTE_EINVAL with the count set when max_leaves is too small). */
+rte_status rte_kdtree_build_host(const float* xyz, int64_t n, int leaf_size, float expand_ratio,
+                                 int64_t max_leaves, float* tight, float* expanded, int32_t* pids,
+                                 int64_t* n_leaves);
+
+/* FP64 symmetric eigendecomposition used by rte_build_pca (pca.cpp:11-29):
+ * a [n x n] row-major; w [n] descending; v [n x n] with eigenvector j in
+ * column j, largest-magnitude component positive. */
+rte_status rte_sym_eig_host(const double* a, int n, double* w, double* v);
+
+/* Message of the last failure on this thread ("" if none). */
+const char* rte_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RTENTRY_H_ */

@@ -1,0 +1,376 @@
+"""rt_entry_gb300 -- GB300 (sm_103a) query path of rt_entry, Python binding.
+
+Thin ctypes layer over the C ABI in ``include/rtentry.h`` (librtentry.so,
+built in-tree by ``rt_entry_gb300.build.build()``).  The compute runs in
+hand-written CUDA kernels; there is no CPU fallback: importing the binding
+without the built library raises.
+
+Arrays may be numpy arrays (host) or torch tensors (host or CUDA).  Results
+come back in the same kind of memory as the queries.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "librtentry.so")
+
+RTE_OK, RTE_EINVAL, RTE_ENOMEM, RTE_EIO, RTE_ECUDA, RTE_ETIMEOUT, RTE_ESTATE = range(7)
+PREC_FP32, PREC_BF16, PREC_FP8 = 0, 1, 2
+ENTRY_RANDOM, ENTRY_KDTREE, ENTRY_LEARNED = 0, 1, 2
+MAX_DIST = np.float32(536870912.0)
+
+# every entry point include/rtentry.h declares
+EXPORTS = (
+    "rte_default_params", "rte_index_from_host", "rte_index_load", "rte_build_pca", "rte_set_pca",
+    "rte_build_kdtree", "rte_project", "rte_locate", "rte_search", "rte_search_projected",
+    "rte_search_counters", "rte_index_get_info", "rte_get_pca", "rte_get_search_base",
+    "rte_get_kdtree", "rte_index_save", "rte_index_load_dir", "rte_index_free", "rte_last_error",
+    "rte_kdtree_build_host", "rte_sym_eig_host", "rte_get_search_base_lowp",
+)
+
+
+class SearchParams(ctypes.Structure):
+    _fields_ = [("k", ctypes.c_int), ("beam", ctypes.c_int), ("search_width", ctypes.c_int),
+                ("max_iter", ctypes.c_int), ("bloom_words", ctypes.c_int),
+                ("bloom_hashes", ctypes.c_int), ("precision", ctypes.c_int),
+                ("rerank", ctypes.c_int), ("entry_mode", ctypes.c_int),
+                ("warps_per_block", ctypes.c_int)]
+
+
+class IndexInfo(ctypes.Structure):
+    _fields_ = [("np", ctypes.c_int64), ("dim", ctypes.c_int), ("search_dim", ctypes.c_int),
+                ("degree", ctypes.c_int), ("has_pca", ctypes.c_int), ("has_kdtree", ctypes.c_int),
+                ("n_leaves", ctypes.c_int64), ("leaf_size", ctypes.c_int),
+                ("expand_ratio", ctypes.c_float), ("has_bf16", ctypes.c_int),
+                ("has_fp8", ctypes.c_int), ("device", ctypes.c_int),
+                ("device_bytes", ctypes.c_int64)]
+
+
+class RteError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"rte status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load librtentry.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: run `python -m rt_entry_gb300.build` "
+                          "(or __graft_entry__.build()) first; there is no CPU fallback")
+    L = ctypes.CDLL(path)
+    P, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    SP = ctypes.POINTER(SearchParams)
+    sig = {
+        "rte_default_params": ([SP], None),
+        "rte_index_from_host": ([P, i64, i32, P, i32, i32, PP], i32),
+        "rte_index_load": ([ctypes.c_char_p, ctypes.c_char_p, i32, PP], i32),
+        "rte_build_pca": ([P, i32], i32),
+        "rte_set_pca": ([P, P, P, i32], i32),
+        "rte_build_kdtree": ([P, i32, ctypes.c_float], i32),
+        "rte_project": ([P, P, i64, P, P], i32),
+        "rte_locate": ([P, P, i64, P, P], i32),
+        "rte_search": ([P, P, i64, SP, P, P, P], i32),
+        "rte_search_projected": ([P, P, P, i64, SP, P, P, P], i32),
+        "rte_search_counters": ([P, P, P, i64, SP, P, P], i32),
+        "rte_index_get_info": ([P, ctypes.POINTER(IndexInfo)], i32),
+        "rte_get_pca": ([P, P, P, P], i32),
+        "rte_get_search_base": ([P, P], i32),
+        "rte_get_kdtree": ([P, P, P, P], i32),
+        "rte_index_save": ([P, ctypes.c_char_p], i32),
+        "rte_index_load_dir": ([ctypes.c_char_p, i32, PP], i32),
+        "rte_index_free": ([P], None),
+        "rte_last_error": ([], ctypes.c_char_p),
+        "rte_kdtree_build_host": ([P, i64, i32, ctypes.c_float, i64, P, P, P,
+                                   ctypes.POINTER(i64)], i32),
+        "rte_sym_eig_host": ([P, i32, P, P], i32),
+        "rte_get_search_base_lowp": ([P, i32, P], i32),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != RTE_OK:
+        raise RteError(rc, load_library().rte_last_error().decode())
+
+
+def default_params(**kw) -> SearchParams:
+    p = SearchParams()
+    load_library().rte_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise TypeError(f"unknown search parameter {k}")
+        setattr(p, k, int(v))
+    return p
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+def _ptr(x):
+    """(pointer, keepalive) of a C-contiguous numpy array or torch tensor."""
+    if x is None:
+        return None, None
+    if _is_torch(x):
+        if not x.is_contiguous():
+            x = x.contiguous()
+        return ctypes.c_void_p(x.data_ptr()), x
+    a = np.ascontiguousarray(x)
+    return a.ctypes.data_as(ctypes.c_void_p), a
+
+
+def _as(x, np_dtype, torch_dtype_name):
+    if _is_torch(x):
+        import torch
+        return x.to(getattr(torch, torch_dtype_name)).contiguous()
+    return np.ascontiguousarray(x, dtype=np_dtype)
+
+
+def _empty_like_kind(ref, shape, np_dtype, torch_dtype_name):
+    if _is_torch(ref):
+        import torch
+        return torch.empty(shape, dtype=getattr(torch, torch_dtype_name), device=ref.device)
+    return np.empty(shape, dtype=np_dtype)
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return ctypes.c_void_p(stream.cuda_stream)
+    return ctypes.c_void_p(int(stream))
+
+
+def kdtree_build_host(xyz, leaf_size: int, expand_ratio: float = 0.2):
+    """Host kd-tree build alone -> (tight [n,6], expanded [n,6], pids [n, leaf_size])."""
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    n = xyz.shape[0]
+    cap = 4 * (n // max(1, leaf_size // 2) + 2)
+    t = np.empty((cap, 6), np.float32)
+    e = np.empty((cap, 6), np.float32)
+    p = np.empty((cap, leaf_size), np.int32)
+    nl = ctypes.c_int64(0)
+    _check(load_library().rte_kdtree_build_host(
+        xyz.ctypes.data_as(ctypes.c_void_p), n, leaf_size, expand_ratio, cap,
+        t.ctypes.data_as(ctypes.c_void_p), e.ctypes.data_as(ctypes.c_void_p),
+        p.ctypes.data_as(ctypes.c_void_p), ctypes.byref(nl)))
+    k = nl.value
+    return t[:k].copy(), e[:k].copy(), p[:k].copy()
+
+
+def sym_eig_host(a):
+    """FP64 eigendecomposition of the build path -> (w descending, V columns)."""
+    a = np.ascontiguousarray(a, np.float64)
+    n = a.shape[0]
+    w = np.empty(n, np.float64)
+    v = np.empty((n, n), np.float64)
+    _check(load_library().rte_sym_eig_host(a.ctypes.data_as(ctypes.c_void_p), n,
+                                           w.ctypes.data_as(ctypes.c_void_p),
+                                           v.ctypes.data_as(ctypes.c_void_p)))
+    return w, v
+
+
+class Index:
+    """One index on one GPU (the reference's Graph, graph.h:10-82)."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    # ---- construction -------------------------------------------------
+    @classmethod
+    def from_arrays(cls, base, graph, device: int = 0) -> "Index":
+        base = _as(base, np.float32, "float32")
+        graph = _as(graph, np.int32, "int32")
+        pb, kb = _ptr(base)
+        pg, kg = _ptr(graph)
+        h = ctypes.c_void_p()
+        _check(load_library().rte_index_from_host(pb, base.shape[0], base.shape[1], pg,
+                                                  graph.shape[1], device, ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def load(cls, base_path: str, graph_path: str, device: int = 0) -> "Index":
+        h = ctypes.c_void_p()
+        _check(load_library().rte_index_load(base_path.encode(), graph_path.encode(), device,
+                                             ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def load_dir(cls, path: str, device: int = 0) -> "Index":
+        h = ctypes.c_void_p()
+        _check(load_library().rte_index_load_dir(path.encode(), device, ctypes.byref(h)))
+        return cls(h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().rte_index_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- build steps ----------------------------------------------------
+    def build_pca(self, keep_dims: int = 0):
+        _check(load_library().rte_build_pca(self._h, keep_dims))
+        return self
+
+    def set_pca(self, mean, rotation, keep_dims: int = 0):
+        m, km = _ptr(np.ascontiguousarray(mean, np.float32))
+        r, kr = _ptr(np.ascontiguousarray(rotation, np.float32))
+        _check(load_library().rte_set_pca(self._h, m, r, keep_dims))
+        return self
+
+    def build_kdtree(self, leaf_size: int, expand_ratio: float = 0.2):
+        _check(load_library().rte_build_kdtree(self._h, leaf_size, expand_ratio))
+        return self
+
+    # ---- queries ----------------------------------------------------------
+    @property
+    def info(self) -> IndexInfo:
+        i = IndexInfo()
+        _check(load_library().rte_index_get_info(self._h, ctypes.byref(i)))
+        return i
+
+    def project(self, queries, stream=None):
+        queries = _as(queries, np.float32, "float32")
+        out = _empty_like_kind(queries, (queries.shape[0], self.info.search_dim), np.float32, "float32")
+        pq, kq = _ptr(queries)
+        po, ko = _ptr(out)
+        _check(load_library().rte_project(self._h, pq, queries.shape[0], po, _stream_ptr(stream)))
+        return out
+
+    def locate(self, projected, stream=None):
+        projected = _as(projected, np.float32, "float32")
+        out = _empty_like_kind(projected, (projected.shape[0],), np.int32, "int32")
+        pp, kp = _ptr(projected)
+        po, ko = _ptr(out)
+        _check(load_library().rte_locate(self._h, pp, projected.shape[0], po, _stream_ptr(stream)))
+        return out
+
+    def _params(self, params, kw):
+        if params is None:
+            params = default_params(**kw)
+        elif kw:
+            raise TypeError("pass either params or keyword parameters")
+        return params
+
+    def _k(self, params):
+        L = 1
+        while L < params.beam:
+            L <<= 1
+        return params.k if params.k else L
+
+    def search(self, queries, params: SearchParams | None = None, stream=None, out_ids=None,
+               out_dists=None, **kw):
+        """Whole query path: projection, entry selection, beam search."""
+        params = self._params(params, kw)
+        queries = _as(queries, np.float32, "float32")
+        nq = queries.shape[0]
+        k = self._k(params)
+        if out_ids is None:
+            out_ids = _empty_like_kind(queries, (nq, k), np.int32, "int32")
+        if out_dists is None:
+            out_dists = _empty_like_kind(queries, (nq, k), np.float32, "float32")
+        pq, kq = _ptr(queries)
+        pi, ki = _ptr(out_ids)
+        pd, kd = _ptr(out_dists)
+        _check(load_library().rte_search(self._h, pq, nq, ctypes.byref(params), pi, pd,
+                                         _stream_ptr(stream)))
+        return out_ids, out_dists
+
+    def search_projected(self, projected, hits=None, params: SearchParams | None = None,
+                         stream=None, **kw):
+        params = self._params(params, kw)
+        projected = _as(projected, np.float32, "float32")
+        nq = projected.shape[0]
+        k = self._k(params)
+        ids = _empty_like_kind(projected, (nq, k), np.int32, "int32")
+        dists = _empty_like_kind(projected, (nq, k), np.float32, "float32")
+        if hits is not None:
+            hits = _as(hits, np.int32, "int32")
+        pp, kp = _ptr(projected)
+        ph, kh = _ptr(hits)
+        pi, ki = _ptr(ids)
+        pd, kd = _ptr(dists)
+        _check(load_library().rte_search_projected(self._h, pp, ph, nq, ctypes.byref(params), pi,
+                                                   pd, _stream_ptr(stream)))
+        return ids, dists
+
+    def counters(self, projected, hits=None, params: SearchParams | None = None, **kw):
+        """Per-query [entries_valid, expanded, dist_evals, iterations]."""
+        params = self._params(params, kw)
+        projected = _as(projected, np.float32, "float32")
+        nq = projected.shape[0]
+        out = np.empty((nq, 4), np.int64)
+        if hits is not None:
+            hits = _as(hits, np.int32, "int32")
+        pp, kp = _ptr(projected)
+        ph, kh = _ptr(hits)
+        po, ko = _ptr(out)
+        _check(load_library().rte_search_counters(self._h, pp, ph, nq, ctypes.byref(params), po,
+                                                  None))
+        return out
+
+    # ---- artifacts --------------------------------------------------------
+    def pca(self):
+        inf = self.info
+        d = inf.dim
+        mean = np.empty(d, np.float32)
+        rot = np.empty((d, d), np.float32)
+        ev = np.empty(d, np.float64)
+        _check(load_library().rte_get_pca(self._h, mean.ctypes.data_as(ctypes.c_void_p),
+                                          rot.ctypes.data_as(ctypes.c_void_p),
+                                          ev.ctypes.data_as(ctypes.c_void_p)))
+        return mean, rot, ev
+
+    def search_base(self):
+        inf = self.info
+        out = np.empty((inf.np, inf.search_dim), np.float32)
+        _check(load_library().rte_get_search_base(self._h, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def search_base_lowp(self, precision: int):
+        """Search-space base as the BF16 (1) / FP8 (2) path computes with it."""
+        inf = self.info
+        out = np.empty((inf.np, inf.search_dim), np.float32)
+        _check(load_library().rte_get_search_base_lowp(self._h, precision,
+                                                       out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def kdtree(self):
+        inf = self.info
+        t = np.empty((inf.n_leaves, 6), np.float32)
+        e = np.empty((inf.n_leaves, 6), np.float32)
+        p = np.empty((inf.n_leaves, inf.leaf_size), np.int32)
+        _check(load_library().rte_get_kdtree(self._h, t.ctypes.data_as(ctypes.c_void_p),
+                                             e.ctypes.data_as(ctypes.c_void_p),
+                                             p.ctypes.data_as(ctypes.c_void_p)))
+        return t, e, p
+
+    def save(self, path: str):
+        _check(load_library().rte_index_save(self._h, path.encode()))

@@ -1,0 +1,775 @@
+// api.cpp -- C ABI of rt_entry_gb300 (include/rtentry.h).
+//
+// The index object owns every device buffer of one index on one GPU.  Query
+// calls allocate their per-call buffers from the device's stream-ordered
+// memory pool (cudaMallocAsync on the caller's stream), so calls on distinct
+// streams do not share scratch and the pool keeps memory warm across calls.
+#include "rtentry.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "host_build.h"
+#include "index_kernels.h"
+#include "io.h"
+#include "search_dispatch.h"
+
+using namespace rte;
+
+namespace {
+
+thread_local std::string g_err;
+
+rte_status fail(rte_status s, const std::string& msg) {
+  g_err = msg;
+  return s;
+}
+
+#define RTE_CUDA(call)                                                                     \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(e_ == cudaErrorMemoryAllocation ? RTE_ENOMEM : RTE_ECUDA,                \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                     \
+  } while (0)
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    reset();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// Device scratch from the stream-ordered pool, released on scope exit
+// (stream-ordered, so the memory is reused only after prior work finishes).
+struct AsyncBuf {
+  void* p = nullptr;
+  cudaStream_t st = nullptr;
+  AsyncBuf() = default;
+  AsyncBuf(const AsyncBuf&) = delete;
+  ~AsyncBuf() {
+    if (p) cudaFreeAsync(p, st);
+  }
+  cudaError_t alloc(size_t bytes, cudaStream_t s) {
+    st = s;
+    if (bytes == 0) bytes = 16;
+    return cudaMallocAsync(&p, bytes, s);
+  }
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+// Host or device memory?  Unregistered host memory reports
+// cudaMemoryTypeUnregistered; pinned host memory cudaMemoryTypeHost.
+bool is_device_ptr(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int chunks_of(int d) { return (d + 31) / 32; }
+
+}  // namespace
+
+struct rte_index {
+  int device = 0;
+  int num_sms = 0;
+  int64_t np = 0;
+  int dim = 0;
+  int degree = 0;
+  DevBuf<float> raw;      // [np][dim] row-major input vectors
+  DevBuf<int32_t> graph;  // [np][degree]
+  // PCA
+  bool has_pca = false;
+  int search_dim = 0;
+  std::vector<double> mean64, eig64, vec64;  // vec64[dim][dim], column = component
+  std::vector<float> mean32, rot32;          // rot32[dim][dim]
+  DevBuf<float> d_mean, d_rot;               // d_rot[dim][search_dim]
+  // search space
+  int C = 0;
+  DevBuf<float> il32;
+  DevBuf<uint16_t> il16;
+  DevBuf<uint8_t> il8;
+  DevBuf<float> scale8;
+  std::vector<float> xyz;  // first three search-space coordinates [np][3]
+  // kd-tree
+  bool has_kdtree = false;
+  KdTree kd;
+  float expand_ratio = 0.f;
+  DevBuf<BvhNode> d_nodes;
+  DevBuf<int32_t> d_pids;
+};
+
+namespace {
+
+size_t index_bytes(const rte_index* x) {
+  return x->raw.bytes() + x->graph.bytes() + x->d_mean.bytes() + x->d_rot.bytes() +
+         x->il32.bytes() + x->il16.bytes() + x->il8.bytes() + x->scale8.bytes() +
+         x->d_nodes.bytes() + x->d_pids.bytes();
+}
+
+// (Re)build the lane-interleaved FP32/BF16/FP8 copies of the search space
+// from a row-major device array [np][search_dim].
+rte_status make_search_space(rte_index* x, const float* rm) {
+  x->C = chunks_of(x->search_dim);
+  const size_t row = 32 * (size_t)x->C;
+  RTE_CUDA(x->il32.alloc(row * x->np));
+  RTE_CUDA(x->il16.alloc(row * x->np));
+  RTE_CUDA(x->il8.alloc(row * x->np));
+  RTE_CUDA(x->scale8.alloc(x->np));
+  DevBuf<float> xyz;
+  RTE_CUDA(xyz.alloc(3 * x->np));
+  if (x->search_dim < 3) RTE_CUDA(cudaMemset(xyz.p, 0, xyz.bytes()));
+  RTE_CUDA(launch_interleave(rm, x->np, x->search_dim, x->C, x->il32.p, x->il16.p, x->il8.p,
+                             x->scale8.p, xyz.p, 0));
+  x->xyz.resize(3 * x->np);
+  RTE_CUDA(cudaMemcpy(x->xyz.data(), xyz.p, xyz.bytes(), cudaMemcpyDeviceToHost));
+  RTE_CUDA(cudaDeviceSynchronize());
+  // a new search space invalidates the kd-tree built on the old one
+  x->has_kdtree = false;
+  x->d_nodes.reset();
+  x->d_pids.reset();
+  return RTE_OK;
+}
+
+rte_status validate_graph(const int32_t* g, int64_t np, int degree) {
+  const int64_t n = np * degree;
+  for (int64_t i = 0; i < n; ++i)
+    if (g[i] < 0 || g[i] > np)
+      return fail(RTE_EINVAL, "graph id out of range [0, np] at row " + std::to_string(i / degree));
+  return RTE_OK;
+}
+
+rte_status create_index(const float* base, int64_t np, int dim, const int32_t* graph, int degree,
+                        int device, rte_index** out) {
+  if (!out) return fail(RTE_EINVAL, "out is NULL");
+  *out = nullptr;
+  if (!base || !graph) return fail(RTE_EINVAL, "base or graph is NULL");
+  if (np <= 0 || np >= INT32_MAX) return fail(RTE_EINVAL, "np must be in [1, 2^31-1)");
+  if (dim <= 0 || dim > 32 * 32) return fail(RTE_EINVAL, "dim must be in [1, 1024]");
+  if (degree <= 0 || (degree & (degree - 1)))
+    return fail(RTE_EINVAL, "graph degree must be a power of two (graph.cu:134)");
+  // host-side checks first, so a bad graph is reported without a device
+  const bool gdev = is_device_ptr(graph);
+  if (!gdev) {
+    rte_status s0 = validate_graph(graph, np, degree);
+    if (s0 != RTE_OK) return s0;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(RTE_ECUDA, "no CUDA device available");
+  }
+  if (device < 0 || device >= ndev) return fail(RTE_EINVAL, "device index out of range");
+  DeviceGuard g(device);
+  std::unique_ptr<rte_index> x(new rte_index());
+  x->device = device;
+  cudaDeviceGetAttribute(&x->num_sms, cudaDevAttrMultiProcessorCount, device);
+  x->np = np;
+  x->dim = dim;
+  x->degree = degree;
+  // stream-ordered pool keeps freed scratch for reuse
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  std::vector<int32_t> hg;
+  const int32_t* gh = graph;
+  if (gdev) {
+    hg.resize((size_t)np * degree);
+    RTE_CUDA(cudaMemcpy(hg.data(), graph, hg.size() * 4, cudaMemcpyDeviceToHost));
+    gh = hg.data();
+    rte_status s1 = validate_graph(gh, np, degree);
+    if (s1 != RTE_OK) return s1;
+  }
+  rte_status s = RTE_OK;
+  RTE_CUDA(x->raw.alloc((size_t)np * dim));
+  RTE_CUDA(cudaMemcpy(x->raw.p, base, x->raw.bytes(), cudaMemcpyDefault));
+  RTE_CUDA(x->graph.alloc((size_t)np * degree));
+  RTE_CUDA(cudaMemcpy(x->graph.p, gh, x->graph.bytes(), cudaMemcpyHostToDevice));
+  x->search_dim = dim;
+  s = make_search_space(x.get(), x->raw.p);
+  if (s != RTE_OK) return s;
+  *out = x.release();
+  return RTE_OK;
+}
+
+int next_pow2(int v) {
+  int p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+struct Plan {
+  int L, k, NL, NB, wpb, grid, prec;
+  size_t smem;
+};
+
+rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t nq, Plan& pl) {
+  if (!prm) return fail(RTE_EINVAL, "params is NULL");
+  if (prm->beam <= 0) return fail(RTE_EINVAL, "beam must be > 0");
+  pl.L = next_pow2(prm->beam);  // graph.cu:53
+  pl.k = prm->k == 0 ? pl.L : prm->k;  // graph.cu:54
+  if (pl.k < 0 || pl.k > pl.L) return fail(RTE_EINVAL, "k must be in [1, beam] (topk <= n_candidates)");
+  if (pl.L < 32 || pl.L > 256) return fail(RTE_EINVAL, "beam must round to 32..256");
+  if (x->degree < 32) return fail(RTE_EINVAL, "graph degree must be >= 32 for the warp kernel");
+  if (prm->search_width <= 0) return fail(RTE_EINVAL, "search_width must be >= 1");
+  const int B = prm->search_width * x->degree;
+  if (B > 256 || (B & (B - 1))) return fail(RTE_EINVAL, "search_width * degree must be a power of two <= 256");
+  if (prm->max_iter < 0) return fail(RTE_EINVAL, "max_iter must be >= 0");
+  if (prm->bloom_words < 32 || prm->bloom_words > 16384 || (prm->bloom_words & (prm->bloom_words - 1)))
+    return fail(RTE_EINVAL, "bloom_words must be a power of two in [32, 16384]");
+  if (prm->bloom_hashes < 1 || prm->bloom_hashes > 10) return fail(RTE_EINVAL, "bloom_hashes must be in [1, 10]");
+  if (prm->precision < 0 || prm->precision > 2) return fail(RTE_EINVAL, "precision must be 0, 1 or 2");
+  if (prm->entry_mode != RTE_ENTRY_RANDOM && prm->entry_mode != RTE_ENTRY_KDTREE)
+    return fail(RTE_EINVAL, "entry_mode must be RTE_ENTRY_RANDOM or RTE_ENTRY_KDTREE here");
+  if (prm->entry_mode == RTE_ENTRY_KDTREE && !x->has_kdtree)
+    return fail(RTE_ESTATE, "kd-tree entries requested before rte_build_kdtree");
+  if (!search_chunks_supported(x->C))
+    return fail(RTE_EINVAL, "search dimension " + std::to_string(x->search_dim) + " has no kernel instantiation");
+  pl.NL = pl.L / 32;
+  pl.NB = B / 32;
+  pl.prec = prm->precision;
+  pl.wpb = prm->warps_per_block > 0 ? prm->warps_per_block : 8;
+  if (pl.wpb > 8) return fail(RTE_EINVAL, "warps_per_block must be <= 8");
+  const int S = std::max(B, pl.L);
+  pl.smem = (size_t)pl.wpb * (prm->bloom_words + 2 * S) * 4;
+  if (pl.smem > 227 * 1024) return fail(RTE_EINVAL, "bloom filter too large for the block's shared memory");
+  const int occ = occupancy_search(x->C, pl.NL, pl.NB, pl.prec, pl.wpb, pl.smem);
+  if (occ <= 0)
+    return fail(RTE_EINVAL, "no kernel instantiation for beam " + std::to_string(pl.L) + ", batch " +
+                                std::to_string(B) + ", precision " + std::to_string(pl.prec));
+  const int64_t need = (nq + pl.wpb - 1) / pl.wpb;
+  pl.grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)x->num_sms * occ));
+  return RTE_OK;
+}
+
+// Projection + locate + search on device buffers.
+rte_status run_query_path(rte_index* x, const float* d_queries, bool already_projected,
+                          const int32_t* d_hits_in, int64_t nq, const rte_search_params* prm,
+                          int32_t* d_ids, float* d_dists, long long* d_counters, cudaStream_t st) {
+  Plan pl;
+  rte_status s = plan_search(x, prm, nq, pl);
+  if (s != RTE_OK) return s;
+  if (nq == 0) return RTE_OK;
+  const float* qp = d_queries;
+  AsyncBuf proj, hitsb, work;
+  if (!already_projected && x->has_pca) {
+    RTE_CUDA(proj.alloc((size_t)nq * x->search_dim * 4, st));
+    RTE_CUDA(launch_project(d_queries, nq, x->dim, x->dim, x->d_mean.p, x->d_rot.p, x->search_dim,
+                            x->search_dim, proj.as<float>(), x->search_dim, st));
+    qp = proj.as<float>();
+  }
+  const int32_t* hits = d_hits_in;
+  if (prm->entry_mode == RTE_ENTRY_KDTREE && !hits) {
+    RTE_CUDA(hitsb.alloc((size_t)nq * 4, st));
+    RTE_CUDA(launch_locate(x->d_nodes.p, qp, nq, x->search_dim, hitsb.as<int32_t>(), st));
+    hits = hitsb.as<int32_t>();
+  }
+  RTE_CUDA(work.alloc(4, st));
+  RTE_CUDA(cudaMemsetAsync(work.p, 0, 4, st));
+  SearchArgs a{};
+  a.base = x->il32.p;
+  a.base_bf16 = x->il16.p;
+  a.base_fp8 = x->il8.p;
+  a.fp8_scale = x->scale8.p;
+  a.queries = qp;
+  a.graph = x->graph.p;
+  a.leaf_pids = x->has_kdtree ? x->d_pids.p : nullptr;
+  a.hits = hits;
+  a.out_ids = d_ids;
+  a.out_dists = d_dists;
+  a.counters = d_counters;
+  a.work = work.as<unsigned int>();
+  a.np = (int)x->np;
+  a.d = x->search_dim;
+  a.qstride = x->search_dim;
+  a.nq = (int)nq;
+  a.R = x->degree;
+  a.W = prm->search_width;
+  a.k = pl.k;
+  a.max_iter = prm->max_iter;
+  a.bloom_words = prm->bloom_words;
+  a.bloom_hashes = prm->bloom_hashes;
+  a.leaf_cap = x->has_kdtree ? x->kd.cap : 1;
+  a.entry_mode = prm->entry_mode;
+  a.rerank = prm->rerank;
+  a.n_leaves = x->has_kdtree ? (int)x->kd.n_leaves : 1;
+  RTE_CUDA(launch_search(a, x->C, pl.NL, pl.NB, pl.prec, pl.wpb, pl.grid, pl.smem, st));
+  return RTE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void rte_default_params(rte_search_params* p) {
+  if (!p) return;
+  p->k = 10;
+  p->beam = 64;
+  p->search_width = 1;
+  p->max_iter = 100;
+  p->bloom_words = 512;
+  p->bloom_hashes = 3;
+  p->precision = RTE_PREC_FP32;
+  p->rerank = 0;
+  p->entry_mode = RTE_ENTRY_KDTREE;
+  p->warps_per_block = 0;
+}
+
+const char* rte_last_error(void) { return g_err.c_str(); }
+
+rte_status rte_index_from_host(const float* base, int64_t np, int dim, const int32_t* graph,
+                               int degree, int device, rte_index** out) {
+  g_err.clear();
+  return create_index(base, np, dim, graph, degree, device, out);
+}
+
+rte_status rte_index_load(const char* base_path, const char* graph_path, int device,
+                          rte_index** out) {
+  g_err.clear();
+  if (!base_path || !graph_path || !out) return fail(RTE_EINVAL, "NULL argument");
+  std::vector<float> base;
+  int64_t np = 0;
+  int dim = 0;
+  std::string err;
+  if (!io::read_vectors(base_path, base, np, dim, err)) return fail(RTE_EIO, err);
+  std::vector<int32_t> graph;
+  int degree = 0;
+  if (!io::read_graph(graph_path, np, graph, degree, err)) return fail(RTE_EIO, err);
+  return create_index(base.data(), np, dim, graph.data(), degree, device, out);
+}
+
+void rte_index_free(rte_index* idx) {
+  if (!idx) return;
+  DeviceGuard g(idx->device);
+  delete idx;
+}
+
+rte_status rte_set_pca(rte_index* x, const float* mean, const float* rotation, int keep_dims) {
+  g_err.clear();
+  if (!x || !mean || !rotation) return fail(RTE_EINVAL, "NULL argument");
+  if (keep_dims == 0) keep_dims = x->dim;
+  if (keep_dims < 3 || keep_dims > x->dim) return fail(RTE_EINVAL, "keep_dims must be in [3, dim]");
+  DeviceGuard g(x->device);
+  const int d = x->dim;
+  x->mean32.assign(mean, mean + d);
+  x->rot32.assign(rotation, rotation + (size_t)d * d);
+  if (x->mean64.size() != (size_t)d) {
+    x->mean64.assign(mean, mean + d);
+    x->vec64.assign(rotation, rotation + (size_t)d * d);
+    x->eig64.assign(d, 0.0);
+  }
+  x->search_dim = keep_dims;
+  std::vector<float> rk((size_t)d * keep_dims);
+  for (int i = 0; i < d; ++i)
+    for (int j = 0; j < keep_dims; ++j) rk[(size_t)i * keep_dims + j] = x->rot32[(size_t)i * d + j];
+  RTE_CUDA(x->d_mean.alloc(d));
+  RTE_CUDA(cudaMemcpy(x->d_mean.p, x->mean32.data(), d * 4, cudaMemcpyHostToDevice));
+  RTE_CUDA(x->d_rot.alloc(rk.size()));
+  RTE_CUDA(cudaMemcpy(x->d_rot.p, rk.data(), rk.size() * 4, cudaMemcpyHostToDevice));
+  DevBuf<float> proj;
+  RTE_CUDA(proj.alloc((size_t)x->np * keep_dims));
+  RTE_CUDA(launch_project(x->raw.p, x->np, d, d, x->d_mean.p, x->d_rot.p, keep_dims, keep_dims,
+                          proj.p, keep_dims, 0));
+  x->has_pca = true;
+  return make_search_space(x, proj.p);
+}
+
+rte_status rte_build_pca(rte_index* x, int keep_dims) {
+  g_err.clear();
+  if (!x) return fail(RTE_EINVAL, "index is NULL");
+  if (x->np < 2) return fail(RTE_EINVAL, "PCA needs at least two vectors");
+  DeviceGuard g(x->device);
+  const int d = x->dim;
+  const int nblocks = (int)std::min<int64_t>(1024, x->np);
+  const int nchunks = (int)std::max<int64_t>(1, std::min<int64_t>(64, x->np / 4096));
+  DevBuf<double> part, mean, cov;
+  RTE_CUDA(part.alloc(std::max<size_t>((size_t)nblocks * d, (size_t)nchunks * d * d)));
+  RTE_CUDA(mean.alloc(d));
+  RTE_CUDA(cov.alloc((size_t)d * d));
+  RTE_CUDA(launch_mean(x->raw.p, x->np, d, part.p, nblocks, mean.p, 0));
+  RTE_CUDA(launch_cov(x->raw.p, x->np, d, mean.p, part.p, nchunks, cov.p, 0));
+  std::vector<double> hmean(d), hcov((size_t)d * d);
+  RTE_CUDA(cudaMemcpy(hmean.data(), mean.p, d * 8, cudaMemcpyDeviceToHost));
+  RTE_CUDA(cudaMemcpy(hcov.data(), cov.p, hcov.size() * 8, cudaMemcpyDeviceToHost));
+  std::vector<double> w(d), v((size_t)d * d);
+  std::string err;
+  if (!sym_eig(hcov.data(), d, w.data(), v.data(), err)) return fail(RTE_EINVAL, err);
+  x->mean64 = hmean;
+  x->eig64 = w;
+  x->vec64 = v;
+  std::vector<float> m32(d), r32((size_t)d * d);
+  for (int i = 0; i < d; ++i) m32[i] = (float)hmean[i];
+  for (size_t i = 0; i < r32.size(); ++i) r32[i] = (float)v[i];
+  return rte_set_pca(x, m32.data(), r32.data(), keep_dims);
+}
+
+rte_status rte_build_kdtree(rte_index* x, int leaf_size, float expand_ratio) {
+  g_err.clear();
+  if (!x) return fail(RTE_EINVAL, "index is NULL");
+  if (leaf_size <= 0) return fail(RTE_EINVAL, "leaf_size must be > 0");
+  if (!(expand_ratio >= 0.f) || !std::isfinite(expand_ratio))
+    return fail(RTE_EINVAL, "expand_ratio must be finite and >= 0");
+  DeviceGuard g(x->device);
+  KdTree t;
+  std::string err;
+  if (!kd_build(x->xyz.data(), x->np, leaf_size, t, err)) return fail(RTE_EINVAL, err);
+  if (t.depth + 2 > kBvhMaxDepth) return fail(RTE_EINVAL, "kd-tree deeper than the locate stack");
+  kd_expand(t, expand_ratio);
+  RTE_CUDA(x->d_nodes.alloc(t.nodes.size()));
+  RTE_CUDA(cudaMemcpy(x->d_nodes.p, t.nodes.data(), x->d_nodes.bytes(), cudaMemcpyHostToDevice));
+  RTE_CUDA(x->d_pids.alloc(t.pids.size()));
+  RTE_CUDA(cudaMemcpy(x->d_pids.p, t.pids.data(), x->d_pids.bytes(), cudaMemcpyHostToDevice));
+  x->kd = std::move(t);
+  x->expand_ratio = expand_ratio;
+  x->has_kdtree = true;
+  return RTE_OK;
+}
+
+rte_status rte_project(rte_index* x, const float* queries, int64_t nq, float* out, void* stream) {
+  g_err.clear();
+  if (!x || (!queries && nq) || (!out && nq)) return fail(RTE_EINVAL, "NULL argument");
+  if (nq < 0) return fail(RTE_EINVAL, "nq < 0");
+  if (nq == 0) return RTE_OK;
+  DeviceGuard g(x->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool qd = is_device_ptr(queries), od = is_device_ptr(out);
+  AsyncBuf qb, ob;
+  const float* dq = queries;
+  if (!qd) {
+    RTE_CUDA(qb.alloc((size_t)nq * x->dim * 4, st));
+    RTE_CUDA(cudaMemcpyAsync(qb.p, queries, (size_t)nq * x->dim * 4, cudaMemcpyHostToDevice, st));
+    dq = qb.as<float>();
+  }
+  float* dout = out;
+  if (!od) {
+    RTE_CUDA(ob.alloc((size_t)nq * x->search_dim * 4, st));
+    dout = ob.as<float>();
+  }
+  if (x->has_pca) {
+    RTE_CUDA(launch_project(dq, nq, x->dim, x->dim, x->d_mean.p, x->d_rot.p, x->search_dim,
+                            x->search_dim, dout, x->search_dim, st));
+  } else {
+    RTE_CUDA(cudaMemcpyAsync(dout, dq, (size_t)nq * x->dim * 4, cudaMemcpyDeviceToDevice, st));
+  }
+  if (!od) {
+    RTE_CUDA(cudaMemcpyAsync(out, dout, (size_t)nq * x->search_dim * 4, cudaMemcpyDeviceToHost, st));
+    RTE_CUDA(cudaStreamSynchronize(st));
+  }
+  return RTE_OK;
+}
+
+rte_status rte_locate(rte_index* x, const float* projected, int64_t nq, int32_t* out_leaf,
+                      void* stream) {
+  g_err.clear();
+  if (!x || (!projected && nq) || (!out_leaf && nq)) return fail(RTE_EINVAL, "NULL argument");
+  if (nq < 0) return fail(RTE_EINVAL, "nq < 0");
+  if (!x->has_kdtree) return fail(RTE_ESTATE, "rte_locate before rte_build_kdtree");
+  if (nq == 0) return RTE_OK;
+  DeviceGuard g(x->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool pd = is_device_ptr(projected), od = is_device_ptr(out_leaf);
+  AsyncBuf pb, ob;
+  const float* dp = projected;
+  if (!pd) {
+    RTE_CUDA(pb.alloc((size_t)nq * x->search_dim * 4, st));
+    RTE_CUDA(cudaMemcpyAsync(pb.p, projected, (size_t)nq * x->search_dim * 4, cudaMemcpyHostToDevice, st));
+    dp = pb.as<float>();
+  }
+  int32_t* dout = out_leaf;
+  if (!od) {
+    RTE_CUDA(ob.alloc((size_t)nq * 4, st));
+    dout = ob.as<int32_t>();
+  }
+  RTE_CUDA(launch_locate(x->d_nodes.p, dp, nq, x->search_dim, dout, st));
+  if (!od) {
+    RTE_CUDA(cudaMemcpyAsync(out_leaf, dout, (size_t)nq * 4, cudaMemcpyDeviceToHost, st));
+    RTE_CUDA(cudaStreamSynchronize(st));
+  }
+  return RTE_OK;
+}
+
+static rte_status search_common(rte_index* x, const float* q, bool projected, const int32_t* hits,
+                                int64_t nq, const rte_search_params* prm, int32_t* out_ids,
+                                float* out_dists, int64_t* counters, void* stream) {
+  if (!x || !prm) return fail(RTE_EINVAL, "NULL argument");
+  if (nq < 0) return fail(RTE_EINVAL, "nq < 0");
+  if (nq > 0 && (!q || (!out_ids && !counters))) return fail(RTE_EINVAL, "NULL argument");
+  if (nq >= INT32_MAX) return fail(RTE_EINVAL, "nq must be < 2^31");
+  DeviceGuard g(x->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  Plan pl;
+  rte_status s = plan_search(x, prm, nq, pl);
+  if (s != RTE_OK) return s;
+  if (nq == 0) return RTE_OK;
+  const int qdim = projected ? x->search_dim : x->dim;
+  const size_t qbytes = (size_t)nq * qdim * 4;
+  const size_t obytes = (size_t)nq * pl.k * 4;
+  bool host_io = false;
+  AsyncBuf qb, hb, ib, db, cb;
+  const float* dq = q;
+  if (!is_device_ptr(q)) {
+    host_io = true;
+    RTE_CUDA(qb.alloc(qbytes, st));
+    RTE_CUDA(cudaMemcpyAsync(qb.p, q, qbytes, cudaMemcpyHostToDevice, st));
+    dq = qb.as<float>();
+  }
+  const int32_t* dh = hits;
+  if (hits && !is_device_ptr(hits)) {
+    host_io = true;
+    RTE_CUDA(hb.alloc((size_t)nq * 4, st));
+    RTE_CUDA(cudaMemcpyAsync(hb.p, hits, (size_t)nq * 4, cudaMemcpyHostToDevice, st));
+    dh = hb.as<int32_t>();
+  }
+  int32_t* di = out_ids;
+  const bool ids_host = out_ids && !is_device_ptr(out_ids);
+  if (!out_ids || ids_host) {
+    RTE_CUDA(ib.alloc(obytes, st));
+    di = ib.as<int32_t>();
+  }
+  float* dd = out_dists;
+  const bool dists_host = out_dists && !is_device_ptr(out_dists);
+  if (dists_host) {
+    RTE_CUDA(db.alloc(obytes, st));
+    dd = db.as<float>();
+  }
+  long long* dc = nullptr;
+  const bool cnt_host = counters && !is_device_ptr(counters);
+  if (counters) {
+    if (cnt_host) {
+      RTE_CUDA(cb.alloc((size_t)nq * 32, st));
+      dc = cb.as<long long>();
+    } else {
+      dc = reinterpret_cast<long long*>(counters);
+    }
+  }
+  s = run_query_path(x, dq, projected, dh, nq, prm, di, dd, dc, st);
+  if (s != RTE_OK) return s;
+  if (ids_host) RTE_CUDA(cudaMemcpyAsync(out_ids, di, obytes, cudaMemcpyDeviceToHost, st));
+  if (dists_host) RTE_CUDA(cudaMemcpyAsync(out_dists, dd, obytes, cudaMemcpyDeviceToHost, st));
+  if (cnt_host) RTE_CUDA(cudaMemcpyAsync(counters, dc, (size_t)nq * 32, cudaMemcpyDeviceToHost, st));
+  if (host_io || ids_host || dists_host || cnt_host) RTE_CUDA(cudaStreamSynchronize(st));
+  return RTE_OK;
+}
+
+rte_status rte_search(rte_index* x, const float* queries, int64_t nq,
+                      const rte_search_params* params, int32_t* out_ids, float* out_dists,
+                      void* stream) {
+  g_err.clear();
+  return search_common(x, queries, false, nullptr, nq, params, out_ids, out_dists, nullptr, stream);
+}
+
+rte_status rte_search_projected(rte_index* x, const float* projected, const int32_t* hits,
+                                int64_t nq, const rte_search_params* params, int32_t* out_ids,
+                                float* out_dists, void* stream) {
+  g_err.clear();
+  return search_common(x, projected, true, hits, nq, params, out_ids, out_dists, nullptr, stream);
+}
+
+rte_status rte_search_counters(rte_index* x, const float* projected, const int32_t* hits,
+                               int64_t nq, const rte_search_params* params, int64_t* counters,
+                               void* stream) {
+  g_err.clear();
+  if (!counters && nq) return fail(RTE_EINVAL, "counters is NULL");
+  return search_common(x, projected, true, hits, nq, params, nullptr, nullptr, counters, stream);
+}
+
+rte_status rte_kdtree_build_host(const float* xyz, int64_t n, int leaf_size, float expand_ratio,
+                                 int64_t max_leaves, float* tight, float* expanded, int32_t* pids,
+                                 int64_t* n_leaves) {
+  g_err.clear();
+  if (!xyz || !n_leaves) return fail(RTE_EINVAL, "NULL argument");
+  if (n <= 0 || n >= INT32_MAX || leaf_size <= 0) return fail(RTE_EINVAL, "bad sizes");
+  KdTree t;
+  std::string err;
+  if (!kd_build(xyz, n, leaf_size, t, err)) return fail(RTE_EINVAL, err);
+  kd_expand(t, expand_ratio);
+  *n_leaves = t.n_leaves;
+  if (t.n_leaves > max_leaves) return fail(RTE_EINVAL, "max_leaves too small");
+  if (tight) std::copy(t.tight.begin(), t.tight.end(), tight);
+  if (expanded) std::copy(t.expanded.begin(), t.expanded.end(), expanded);
+  if (pids) std::copy(t.pids.begin(), t.pids.end(), pids);
+  return RTE_OK;
+}
+
+rte_status rte_sym_eig_host(const double* a, int n, double* w, double* v) {
+  g_err.clear();
+  if (!a || !w || !v || n <= 0) return fail(RTE_EINVAL, "bad argument");
+  std::string err;
+  if (!sym_eig(a, n, w, v, err)) return fail(RTE_EINVAL, err);
+  return RTE_OK;
+}
+
+rte_status rte_index_get_info(const rte_index* x, rte_index_info* info) {
+  g_err.clear();
+  if (!x || !info) return fail(RTE_EINVAL, "NULL argument");
+  info->np = x->np;
+  info->dim = x->dim;
+  info->search_dim = x->search_dim;
+  info->degree = x->degree;
+  info->has_pca = x->has_pca;
+  info->has_kdtree = x->has_kdtree;
+  info->n_leaves = x->has_kdtree ? x->kd.n_leaves : 0;
+  info->leaf_size = x->has_kdtree ? x->kd.cap : 0;
+  info->expand_ratio = x->expand_ratio;
+  info->has_bf16 = x->il16.p != nullptr;
+  info->has_fp8 = x->il8.p != nullptr;
+  info->device = x->device;
+  info->device_bytes = (int64_t)index_bytes(x);
+  return RTE_OK;
+}
+
+rte_status rte_get_pca(const rte_index* x, float* mean, float* rotation, double* eigvals) {
+  g_err.clear();
+  if (!x) return fail(RTE_EINVAL, "index is NULL");
+  if (!x->has_pca) return fail(RTE_ESTATE, "no PCA built");
+  if (mean) std::copy(x->mean32.begin(), x->mean32.end(), mean);
+  if (rotation) std::copy(x->rot32.begin(), x->rot32.end(), rotation);
+  if (eigvals) std::copy(x->eig64.begin(), x->eig64.end(), eigvals);
+  return RTE_OK;
+}
+
+rte_status rte_get_search_base(const rte_index* x, float* out) {
+  g_err.clear();
+  if (!x || !out) return fail(RTE_EINVAL, "NULL argument");
+  DeviceGuard g(x->device);
+  DevBuf<float> tmp;
+  RTE_CUDA(tmp.alloc((size_t)x->np * x->search_dim));
+  RTE_CUDA(launch_deinterleave(x->il32.p, x->np, x->search_dim, x->C, tmp.p, 0));
+  RTE_CUDA(cudaMemcpy(out, tmp.p, tmp.bytes(), cudaMemcpyDefault));
+  return RTE_OK;
+}
+
+rte_status rte_get_search_base_lowp(const rte_index* x, int precision, float* out) {
+  g_err.clear();
+  if (!x || !out) return fail(RTE_EINVAL, "NULL argument");
+  if (precision != RTE_PREC_BF16 && precision != RTE_PREC_FP8)
+    return fail(RTE_EINVAL, "precision must be RTE_PREC_BF16 or RTE_PREC_FP8");
+  DeviceGuard g(x->device);
+  DevBuf<float> tmp;
+  RTE_CUDA(tmp.alloc((size_t)x->np * x->search_dim));
+  const void* src = precision == RTE_PREC_BF16 ? (const void*)x->il16.p : (const void*)x->il8.p;
+  RTE_CUDA(launch_dequant(src, x->scale8.p, precision, x->np, x->search_dim, x->C, tmp.p, 0));
+  RTE_CUDA(cudaMemcpy(out, tmp.p, tmp.bytes(), cudaMemcpyDefault));
+  return RTE_OK;
+}
+
+rte_status rte_get_kdtree(const rte_index* x, float* tight, float* expanded, int32_t* pids) {
+  g_err.clear();
+  if (!x) return fail(RTE_EINVAL, "index is NULL");
+  if (!x->has_kdtree) return fail(RTE_ESTATE, "no kd-tree built");
+  if (tight) std::copy(x->kd.tight.begin(), x->kd.tight.end(), tight);
+  if (expanded) std::copy(x->kd.expanded.begin(), x->kd.expanded.end(), expanded);
+  if (pids) std::copy(x->kd.pids.begin(), x->kd.pids.end(), pids);
+  return RTE_OK;
+}
+
+rte_status rte_index_save(const rte_index* x, const char* dir) {
+  g_err.clear();
+  if (!x || !dir) return fail(RTE_EINVAL, "NULL argument");
+  DeviceGuard g(x->device);
+  std::string err;
+  std::vector<float> raw((size_t)x->np * x->dim);
+  RTE_CUDA(cudaMemcpy(raw.data(), x->raw.p, raw.size() * 4, cudaMemcpyDeviceToHost));
+  std::vector<int32_t> graph((size_t)x->np * x->degree);
+  RTE_CUDA(cudaMemcpy(graph.data(), x->graph.p, graph.size() * 4, cudaMemcpyDeviceToHost));
+  io::IndexFiles f;
+  f.np = x->np;
+  f.dim = x->dim;
+  f.degree = x->degree;
+  f.base = &raw;
+  f.graph = &graph;
+  std::vector<float> pca_base;
+  if (x->has_pca) {
+    f.has_pca = true;
+    f.search_dim = x->search_dim;
+    f.mean = &x->mean32;
+    f.rot = &x->rot32;
+    pca_base.resize((size_t)x->np * x->search_dim);
+    DevBuf<float> tmp;
+    RTE_CUDA(tmp.alloc(pca_base.size()));
+    RTE_CUDA(launch_deinterleave(x->il32.p, x->np, x->search_dim, x->C, tmp.p, 0));
+    RTE_CUDA(cudaMemcpy(pca_base.data(), tmp.p, tmp.bytes(), cudaMemcpyDeviceToHost));
+    f.pca_base = &pca_base;
+  }
+  if (x->has_kdtree) {
+    f.has_kdtree = true;
+    f.leaf_size = x->kd.cap;
+    f.expand_ratio = x->expand_ratio;
+    f.n_leaves = x->kd.n_leaves;
+    f.tight = &x->kd.tight;
+    f.pids = &x->kd.pids;
+  }
+  if (!io::save_index(dir, f, err)) return fail(RTE_EIO, err);
+  return RTE_OK;
+}
+
+rte_status rte_index_load_dir(const char* dir, int device, rte_index** out) {
+  g_err.clear();
+  if (!dir || !out) return fail(RTE_EINVAL, "NULL argument");
+  io::LoadedIndex L;
+  std::string err;
+  if (!io::load_index(dir, L, err)) return fail(RTE_EIO, err);
+  rte_status s = create_index(L.base.data(), L.np, L.dim, L.graph.data(), L.degree, device, out);
+  if (s != RTE_OK) return s;
+  if (L.has_pca) {
+    s = rte_set_pca(*out, L.mean.data(), L.rot.data(), L.search_dim);
+    if (s != RTE_OK) {
+      rte_index_free(*out);
+      *out = nullptr;
+      return s;
+    }
+  }
+  if (L.has_kdtree) {
+    s = rte_build_kdtree(*out, L.leaf_size, L.expand_ratio);
+    if (s != RTE_OK) {
+      rte_index_free(*out);
+      *out = nullptr;
+      return s;
+    }
+  }
+  return RTE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,320 @@
+// index_kernels.cu -- build-side and entry-stage kernels for sm_103a.
+//
+//   mean/covariance  FP64, deterministic (fixed row chunks, fixed reduction
+//                    order).  The reference forms C = X^T X / (n-1) of the
+//                    centred base in FP64 with Eigen on one host thread
+//                    (pca.cpp:4-10,44-48).
+//   projection       out = (X - mean) V[:, :k], FP32 accumulation.  Used for
+//                    the base (pca.cpp:122-126, which does it in FP64 on the
+//                    host) and for the queries (graph.cu:258-273, a cuBLAS
+//                    FP32 GEMM with the mean term folded in via beta = -1).
+//   interleave       row-major FP32 -> lane-interleaved FP32 / BF16 / FP8-E4M3
+//                    (layout.cuh), plus the first three coordinates for the
+//                    kd-tree.
+//   locate           smallest-index expanded leaf box containing a point,
+//                    0 on a miss; replaces the OptiX ray cast
+//                    (devicePrograms.cu:29-96, raytracing.cpp:283-334).
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
+#include <stdint.h>
+
+#include "index_kernels.h"
+#include "layout.cuh"
+
+namespace rte {
+
+// ---------------------------------------------------------------- mean ----
+// Block b sums rows [b*rows_per_block, ...) of every column in FP64 into
+// partial[b][col]; a second kernel adds the partials in block order.
+__global__ void col_sum_partial(const float* __restrict__ x, int64_t n, int d,
+                                int64_t rows_per_block, double* __restrict__ partial) {
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per_block;
+  const int64_t r1 = min(n, r0 + rows_per_block);
+  for (int c = threadIdx.x; c < d; c += blockDim.x) {
+    double s = 0.0;
+    for (int64_t r = r0; r < r1; ++r) s += (double)x[r * d + c];
+    partial[(int64_t)blockIdx.x * d + c] = s;
+  }
+}
+
+__global__ void col_sum_finish(const double* __restrict__ partial, int nblocks, int d, int64_t n,
+                               double* __restrict__ mean) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d) return;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; ++b) s += partial[(int64_t)b * d + c];
+  mean[c] = s / (double)n;
+}
+
+// ---------------------------------------------------------- covariance ----
+// Tile of 32x32 outputs per block (16x16 threads, 2x2 each) over a chunk of
+// rows; rows are centred in FP64 as they are staged in shared memory.
+constexpr int kCovTile = 32;
+constexpr int kCovK = 32;
+
+__global__ void cov_partial(const float* __restrict__ x, int64_t n, int d,
+                            const double* __restrict__ mean, int64_t rows_per_chunk,
+                            double* __restrict__ partial) {
+  __shared__ double sa[kCovK][kCovTile + 1];
+  __shared__ double sb[kCovK][kCovTile + 1];
+  const int i0 = blockIdx.y * kCovTile, j0 = blockIdx.x * kCovTile;
+  const int64_t r0 = (int64_t)blockIdx.z * rows_per_chunk;
+  const int64_t r1 = min(n, r0 + rows_per_chunk);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  double acc[2][2] = {{0, 0}, {0, 0}};
+  for (int64_t rb = r0; rb < r1; rb += kCovK) {
+    for (int t = ty * 16 + tx; t < kCovK * kCovTile; t += 256) {
+      const int rr = t / kCovTile, cc = t % kCovTile;
+      const int64_t r = rb + rr;
+      double va = 0.0, vb = 0.0;
+      if (r < r1) {
+        if (i0 + cc < d) va = (double)x[r * d + i0 + cc] - mean[i0 + cc];
+        if (j0 + cc < d) vb = (double)x[r * d + j0 + cc] - mean[j0 + cc];
+      }
+      sa[rr][cc] = va;
+      sb[rr][cc] = vb;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int k = 0; k < kCovK; ++k) {
+      const double a0 = sa[k][ty], a1 = sa[k][ty + 16];
+      const double b0 = sb[k][tx], b1 = sb[k][tx + 16];
+      acc[0][0] = fma(a0, b0, acc[0][0]);
+      acc[0][1] = fma(a0, b1, acc[0][1]);
+      acc[1][0] = fma(a1, b0, acc[1][0]);
+      acc[1][1] = fma(a1, b1, acc[1][1]);
+    }
+    __syncthreads();
+  }
+  double* out = partial + (int64_t)blockIdx.z * d * d;
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) {
+      const int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
+      if (i < d && j < d) out[(int64_t)i * d + j] = acc[a][b];
+    }
+}
+
+__global__ void cov_finish(const double* __restrict__ partial, int nchunks, int d, int64_t n,
+                           double* __restrict__ cov) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t dd = (int64_t)d * d;
+  if (e >= dd) return;
+  double s = 0.0;
+  for (int c = 0; c < nchunks; ++c) s += partial[c * dd + e];
+  cov[e] = s / (double)(n - 1);
+}
+
+// ---------------------------------------------------------- projection ----
+// out[r][j] = sum_c (x[r][c] - mean[c]) * V[c][j] for j < k, FP32 FMA chain
+// in c order.  64 rows x 32 columns per block; x and V staged in shared
+// memory in 32-wide slices of c.
+constexpr int kPrRows = 64;
+constexpr int kPrCols = 32;
+constexpr int kPrK = 32;
+
+__global__ void project_rows(const float* __restrict__ x, int64_t n, int d, int xstride,
+                             const float* __restrict__ mean, const float* __restrict__ V, int vstride,
+                             int k, float* __restrict__ out, int ostride) {
+  __shared__ float sx[kPrRows][kPrK + 1];
+  __shared__ float sv[kPrK][kPrCols];
+  const int64_t row0 = (int64_t)blockIdx.x * kPrRows;
+  const int col0 = blockIdx.y * kPrCols;
+  const int tx = threadIdx.x & 31;   // column
+  const int ty = threadIdx.x >> 5;   // 8 row groups
+  float acc[kPrRows / 8];
+#pragma unroll
+  for (int i = 0; i < kPrRows / 8; ++i) acc[i] = 0.0f;
+  for (int c0 = 0; c0 < d; c0 += kPrK) {
+    for (int t = threadIdx.x; t < kPrRows * kPrK; t += blockDim.x) {
+      const int rr = t / kPrK, cc = t % kPrK;
+      const int64_t r = row0 + rr;
+      float v = 0.0f;
+      if (r < n && c0 + cc < d) v = __fsub_rn(x[r * xstride + c0 + cc], mean ? mean[c0 + cc] : 0.0f);
+      sx[rr][cc] = v;
+    }
+    for (int t = threadIdx.x; t < kPrK * kPrCols; t += blockDim.x) {
+      const int cc = t / kPrCols, jj = t % kPrCols;
+      float v = 0.0f;
+      if (c0 + cc < d && col0 + jj < k) v = V[(int64_t)(c0 + cc) * vstride + col0 + jj];
+      sv[cc][jj] = v;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int cc = 0; cc < kPrK; ++cc) {
+      const float vv = sv[cc][tx];
+#pragma unroll
+      for (int i = 0; i < kPrRows / 8; ++i) acc[i] = __fmaf_rn(sx[ty + 8 * i][cc], vv, acc[i]);
+    }
+    __syncthreads();
+  }
+  const int j = col0 + tx;
+  if (j < k)
+#pragma unroll
+    for (int i = 0; i < kPrRows / 8; ++i) {
+      const int64_t r = row0 + ty + 8 * i;
+      if (r < n) out[r * ostride + j] = acc[i];
+    }
+}
+
+// ---------------------------------------------------------- interleave ----
+__global__ void interleave_rows(const float* __restrict__ src, int64_t n, int d, int C,
+                                float* __restrict__ il32, __nv_bfloat16* __restrict__ il16,
+                                uint8_t* __restrict__ il8, float* __restrict__ scale8,
+                                float* __restrict__ xyz) {
+  // one warp per row
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n; r += nwarps) {
+    const float* s = src + r * d;
+    float amax = 0.0f;
+    for (int c = 0; c < C; ++c) {
+      const int dim = lane + 32 * c;
+      const float v = dim < d ? s[dim] : 0.0f;
+      amax = fmaxf(amax, fabsf(v));
+      const int64_t o = r * (32 * C) + interleaved_offset(c, lane, C);
+      if (il32) il32[o] = v;
+      if (il16) il16[o] = __float2bfloat16_rn(v);
+    }
+    if (il8) {
+      for (int off = 16; off >= 1; off >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, off));
+      const float sc = amax > 0.0f ? amax / 448.0f : 1.0f;
+      if (lane == 0) scale8[r] = sc;
+      for (int c = 0; c < C; ++c) {
+        const int dim = lane + 32 * c;
+        const float v = dim < d ? s[dim] : 0.0f;
+        const int64_t o = r * (32 * C) + interleaved_offset(c, lane, C);
+        il8[o] = (uint8_t)__nv_cvt_float_to_fp8(__fdiv_rn(v, sc), __NV_SATFINITE, __NV_E4M3);
+      }
+    }
+    if (xyz && lane < 3) xyz[r * 3 + lane] = lane < d ? s[lane] : 0.0f;
+  }
+}
+
+__global__ void deinterleave_rows(const float* __restrict__ il32, int64_t n, int d, int C,
+                                  float* __restrict__ dst) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n; r += nwarps)
+    for (int c = 0; c < C; ++c) {
+      const int dim = lane + 32 * c;
+      if (dim < d) dst[r * d + dim] = il32[r * (32 * C) + interleaved_offset(c, lane, C)];
+    }
+}
+
+// The values the BF16 / FP8 search paths compute with, de-interleaved:
+// exactly the widening done by load_interleaved_bf16 / _fp8 (and the FP8
+// scale multiply of the search kernel's row loader).
+__global__ void dequant_rows(const void* __restrict__ il, const float* __restrict__ scale8,
+                             int precision, int64_t n, int d, int C, float* __restrict__ dst) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n; r += nwarps)
+    for (int c = 0; c < C; ++c) {
+      const int dim = lane + 32 * c;
+      if (dim >= d) continue;
+      const int64_t o = r * (32 * C) + interleaved_offset(c, lane, C);
+      float v;
+      if (precision == 1) {
+        v = __uint_as_float((uint32_t)reinterpret_cast<const uint16_t*>(il)[o] << 16);
+      } else {
+        const uint8_t b = reinterpret_cast<const uint8_t*>(il)[o];
+        v = fp8x2_to_float2((uint16_t)b).x * scale8[r];
+      }
+      dst[r * d + dim] = v;
+    }
+}
+
+// -------------------------------------------------------------- locate ----
+// Pre-order, left-first traversal of the kd-tree with each node bounded by
+// the union of its leaves' expanded boxes.  Leaves are numbered in the same
+// order, so the first leaf whose box contains the point is the smallest such
+// index (canonical rule for the ray cast's arbitrary hit).
+__global__ void locate_points(const BvhNode* __restrict__ nodes, const float* __restrict__ pts,
+                              int64_t n, int stride, int32_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float x = pts[i * stride + 0], y = pts[i * stride + 1], z = pts[i * stride + 2];
+  int stack[kBvhMaxDepth];
+  int sp = 0;
+  stack[sp++] = 0;
+  int32_t hit = 0;
+  while (sp > 0) {
+    const BvhNode nd = nodes[stack[--sp]];
+    if (!(nd.lo[0] <= x && x <= nd.hi[0] && nd.lo[1] <= y && y <= nd.hi[1] && nd.lo[2] <= z &&
+          z <= nd.hi[2]))
+      continue;
+    if (nd.left < 0) {
+      hit = -nd.left - 1;
+      break;
+    }
+    if (sp + 2 > kBvhMaxDepth) break;  // depth is bounded by the build
+    stack[sp++] = nd.right;
+    stack[sp++] = nd.left;
+  }
+  out[i] = hit;
+}
+
+// -------------------------------------------------------------- launches ----
+cudaError_t launch_mean(const float* x, int64_t n, int d, double* partial, int nblocks,
+                        double* mean, cudaStream_t st) {
+  const int64_t rpb = (n + nblocks - 1) / nblocks;
+  col_sum_partial<<<nblocks, 128, 0, st>>>(x, n, d, rpb, partial);
+  col_sum_finish<<<(d + 127) / 128, 128, 0, st>>>(partial, nblocks, d, n, mean);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cov(const float* x, int64_t n, int d, const double* mean, double* partial,
+                       int nchunks, double* cov, cudaStream_t st) {
+  const int64_t rpc = (n + nchunks - 1) / nchunks;
+  dim3 grid((d + kCovTile - 1) / kCovTile, (d + kCovTile - 1) / kCovTile, nchunks);
+  cov_partial<<<grid, dim3(16, 16), 0, st>>>(x, n, d, mean, rpc, partial);
+  const int64_t dd = (int64_t)d * d;
+  cov_finish<<<(unsigned)((dd + 255) / 256), 256, 0, st>>>(partial, nchunks, d, n, cov);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const float* mean,
+                           const float* V, int vstride, int k, float* out, int ostride,
+                           cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
+  project_rows<<<grid, 256, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_interleave(const float* src, int64_t n, int d, int C, float* il32,
+                              void* il16, uint8_t* il8, float* scale8, float* xyz,
+                              cudaStream_t st) {
+  const int64_t blocks = std::min<int64_t>((n + 7) / 8, 65535 * 8);
+  interleave_rows<<<(unsigned)blocks, 256, 0, st>>>(src, n, d, C, il32,
+                                                    reinterpret_cast<__nv_bfloat16*>(il16), il8,
+                                                    scale8, xyz);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_deinterleave(const float* il32, int64_t n, int d, int C, float* dst,
+                                cudaStream_t st) {
+  const int64_t blocks = std::min<int64_t>((n + 7) / 8, 65535 * 8);
+  deinterleave_rows<<<(unsigned)blocks, 256, 0, st>>>(il32, n, d, C, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dequant(const void* il, const float* scale8, int precision, int64_t n, int d,
+                           int C, float* dst, cudaStream_t st) {
+  const int64_t blocks = std::min<int64_t>((n + 7) / 8, 65535 * 8);
+  dequant_rows<<<(unsigned)blocks, 256, 0, st>>>(il, scale8, precision, n, d, C, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_locate(const BvhNode* nodes, const float* pts, int64_t n, int stride,
+                          int32_t* out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  locate_points<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(nodes, pts, n, stride, out);
+  return cudaGetLastError();
+}
+
+}  // namespace rte

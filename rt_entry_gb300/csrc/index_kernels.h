@@ -1,0 +1,38 @@
+// index_kernels.h -- launches of the build-side and entry-stage kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+namespace rte {
+
+// kd-tree node for point location: bound = union of the expanded boxes of
+// the leaves below it.  left < 0 marks a leaf with index -left-1.
+struct BvhNode {
+  float lo[3];
+  float hi[3];
+  int32_t left;
+  int32_t right;
+};
+static_assert(sizeof(BvhNode) == 32, "BvhNode is 32 bytes");
+
+constexpr int kBvhMaxDepth = 64;
+
+cudaError_t launch_mean(const float* x, int64_t n, int d, double* partial, int nblocks,
+                        double* mean, cudaStream_t st);
+cudaError_t launch_cov(const float* x, int64_t n, int d, const double* mean, double* partial,
+                       int nchunks, double* cov, cudaStream_t st);
+cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const float* mean,
+                           const float* V, int vstride, int k, float* out, int ostride,
+                           cudaStream_t st);
+cudaError_t launch_interleave(const float* src, int64_t n, int d, int C, float* il32, void* il16,
+                              uint8_t* il8, float* scale8, float* xyz, cudaStream_t st);
+cudaError_t launch_deinterleave(const float* il32, int64_t n, int d, int C, float* dst,
+                                cudaStream_t st);
+cudaError_t launch_dequant(const void* il, const float* scale8, int precision, int64_t n, int d,
+                           int C, float* dst, cudaStream_t st);
+cudaError_t launch_locate(const BvhNode* nodes, const float* pts, int64_t n, int stride,
+                          int32_t* out, cudaStream_t st);
+
+}  // namespace rte

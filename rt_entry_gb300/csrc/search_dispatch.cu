@@ -1,0 +1,74 @@
+// search_dispatch.cu -- maps (chunks, precision) to the instantiation files.
+#include "search_dispatch.h"
+
+namespace rte {
+
+void* search_lookup_c1_f32(int, int);
+void* search_lookup_c2_f32(int, int);
+void* search_lookup_c3_f32(int, int);
+void* search_lookup_c3_bf16(int, int);
+void* search_lookup_c3_fp8(int, int);
+void* search_lookup_c4_f32(int, int);
+void* search_lookup_c4_bf16(int, int);
+void* search_lookup_c4_fp8(int, int);
+void* search_lookup_c30_f32(int, int);
+void* search_lookup_c30_bf16(int, int);
+void* search_lookup_c30_fp8(int, int);
+
+namespace {
+struct Entry {
+  int C;
+  KernelLookup f32, bf16, fp8;
+};
+const Entry kTable[] = {
+    {1, search_lookup_c1_f32, nullptr, nullptr},
+    {2, search_lookup_c2_f32, nullptr, nullptr},
+    {3, search_lookup_c3_f32, search_lookup_c3_bf16, search_lookup_c3_fp8},
+    {4, search_lookup_c4_f32, search_lookup_c4_bf16, search_lookup_c4_fp8},
+    {30, search_lookup_c30_f32, search_lookup_c30_bf16, search_lookup_c30_fp8},
+};
+}  // namespace
+
+bool search_chunks_supported(int C) {
+  for (const Entry& e : kTable)
+    if (e.C == C) return true;
+  return false;
+}
+
+void* search_kernel_ptr(int C, int NL, int NB, int prec) {
+  for (const Entry& e : kTable) {
+    if (e.C != C) continue;
+    KernelLookup f = prec == kPrecF32 ? e.f32 : prec == kPrecBF16 ? e.bf16 : prec == kPrecFP8 ? e.fp8 : nullptr;
+    return f ? f(NL, NB) : nullptr;
+  }
+  return nullptr;
+}
+
+cudaError_t launch_search(const SearchArgs& a, int C, int NL, int NB, int prec, int wpb, int grid,
+                          size_t smem, cudaStream_t st) {
+  void* k = search_kernel_ptr(C, NL, NB, prec);
+  if (!k) return cudaErrorInvalidValue;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  SearchArgs args = a;
+  void* params[] = {&args};
+  return cudaLaunchKernel(k, dim3(grid), dim3(32 * wpb), params, smem, st);
+}
+
+int occupancy_search(int C, int NL, int NB, int prec, int wpb, size_t smem) {
+  void* k = search_kernel_ptr(C, NL, NB, prec);
+  if (!k) return 0;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 32 * wpb, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+}  // namespace rte

@@ -1,0 +1,554 @@
+// search_kernel.cuh -- persistent warp-per-query beam search for sm_103a.
+//
+// Computes exactly what the reference's GraphSearchKernel computes
+// (graph_search.cuh:56-1964, one 64-thread block per query), reorganised for
+// one warp per query:
+//   * the pool (L = 32*NL slots) and the batch (B = 32*NB slots) live in
+//     registers: slot p sits in lane p%32, register p/32.  The reference's
+//     comparator network (bitonic batch sort, pool/batch merge, half-cleaner,
+//     graph_search.cuh:888-957 and :1424-1493) runs on those registers,
+//     across lanes through shuffles and inside a lane for distances >= 32;
+//   * base rows are stored lane-interleaved (see layout.cuh): one 128-bit
+//     load gives lane l the dims l, l+32, l+64, l+96 -- exactly the dims the
+//     reference's reduction tree assigns to lane l -- so a neighbour row is a
+//     single fully coalesced 512-byte gather at d = 128;
+//   * distances of up to 16 neighbours are reduced together by a butterfly
+//     whose every addition pairs the same partial sums as the reference's
+//     shuffle-down tree (16,8,4,2,1), so the results are bit-identical while
+//     using one shuffle per neighbour instead of five;
+//   * the visited-set bloom filter lives in shared memory per warp, sized at
+//     run time (the reference fixes 512 words, graph_search.cuh:4-5);
+//   * warps pull queries from an atomic counter until none are left.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
+#include <stdint.h>
+
+#include "layout.cuh"
+#include "search_types.h"
+
+namespace rte {
+
+constexpr float kMaxDist = 536870912.0f;  // (float)0x1fffffff, structure_on_device.cuh:6
+constexpr unsigned kFull = 0xffffffffu;
+
+// Bloom-filter hash multipliers (graph_search.cuh:89-97).
+__constant__ uint32_t c_hash_mul[20] = {
+    0x924ed183U, 0xd854fc0aU, 0xecf5e3b7U, 0x1bead407U, 0x28a30449U,
+    0xbfc4d99fU, 0x715030e2U, 0xffcfb45bU, 0x6e4ce166U, 0xeb53c362U,
+    0xa93c4f40U, 0xcecde0a4U, 0x0288592dU, 0x362c37bcU, 0x9d4824f0U,
+    0xfdbdd68bU, 0x63258c85U, 0x6726905cU, 0x609500f9U, 0x4de48422U};
+
+
+__device__ __forceinline__ uint32_t bloom_hash(int h, uint32_t x, uint32_t mask_bits) {
+  // hash_ (graph_search.cuh:13-22); x % (SIZE<<5) with SIZE a power of two.
+  x ^= x >> 16;
+  x *= c_hash_mul[h << 1];
+  x ^= x >> 13;
+  x *= c_hash_mul[(h << 1) + 1];
+  x ^= x >> 16;
+  return x & mask_bits;
+}
+
+struct Bloom {
+  uint32_t* w;
+  uint32_t words_mask;  // words - 1
+  uint32_t bits_mask;   // 32*words - 1
+  int lw;               // log2(words)
+  int nh;
+  // set_bit / test_bit: word x % SIZE, bit x / SIZE (graph_search.cuh:7-28).
+  __device__ __forceinline__ void add(uint32_t x) const {
+    for (int h = 0; h < nh; ++h) {
+      uint32_t b = bloom_hash(h, x, bits_mask);
+      atomicOr(&w[b & words_mask], 1u << (b >> lw));
+    }
+  }
+  __device__ __forceinline__ bool test(uint32_t x) const {
+    bool ok = true;
+    for (int h = 0; h < nh; ++h) {
+      uint32_t b = bloom_hash(h, x, bits_mask);
+      ok &= ((w[b & words_mask] >> (b >> lw)) & 1u) != 0;
+    }
+    return ok;
+  }
+  __device__ __forceinline__ void clear(int lane) const {
+    for (uint32_t i = lane; i <= words_mask; i += 32) w[i] = 0u;
+  }
+};
+
+template <int N>
+__device__ __forceinline__ int pick(const int (&a)[N], int c) {
+  int v = a[0];
+#pragma unroll
+  for (int j = 1; j < N; ++j)
+    if (c == j) v = a[j];
+  return v;
+}
+
+// Compare-exchange of slot p with slot p^sub held by another lane (sub < 32).
+// `desc` is the direction of the pair; both lanes evaluate the same
+// predicate on (lower, upper), so ties never swap (strict comparisons).
+__device__ __forceinline__ void cx_lanes(float& d, int& id, int sub, bool desc, int lane) {
+  float od = __shfl_xor_sync(kFull, d, sub);
+  int oi = __shfl_xor_sync(kFull, id, sub);
+  bool lower = (lane & sub) == 0;
+  float da = lower ? d : od;
+  float db = lower ? od : d;
+  bool sw = desc ? (da < db) : (da > db);
+  if (sw) {
+    d = od;
+    id = oi;
+  }
+}
+
+__device__ __forceinline__ void cx_regs(float& da, int& ia, float& db, int& ib, bool desc) {
+  bool sw = desc ? (da < db) : (da > db);
+  if (sw) {
+    float t = da;
+    da = db;
+    db = t;
+    int u = ia;
+    ia = ib;
+    ib = u;
+  }
+}
+
+// Bitonic sort of 32*NB slots (graph_search.cuh:888-919).  With DESC_FINAL
+// the pair (a, a+sub) is descending when a's 2*step block index is even, so
+// the result is descending, as the reference sorts its batch; otherwise the
+// directions are mirrored and the result is ascending.
+template <int NB, bool DESC_FINAL = true>
+__device__ __forceinline__ void sort_batch_desc(float (&d)[NB], int (&id)[NB], int lane) {
+  constexpr int B = 32 * NB;
+#pragma unroll
+  for (int step = 1; step <= B / 2; step <<= 1) {
+#pragma unroll
+    for (int sub = step; sub >= 1; sub >>= 1) {
+      if (sub >= 32) {
+        const int rs = sub >> 5;
+#pragma unroll
+        for (int j = 0; j < NB; ++j) {
+          if (j & rs) continue;
+          const bool desc = (((j << 5) & (2 * step)) == 0) == DESC_FINAL;
+          cx_regs(d[j], id[j], d[j + rs], id[j + rs], desc);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < NB; ++j) {
+          const bool desc = ((((j << 5) + lane) & (2 * step)) == 0) == DESC_FINAL;
+          cx_lanes(d[j], id[j], sub, desc, lane);
+        }
+      }
+    }
+  }
+}
+
+// Pool/batch merge then the ascending half-cleaner (graph_search.cuh:921-957,
+// :1454-1493).  Pool slot L-n+i meets batch slot B-n+i (n = min(L,B)); both
+// are in the same lane.  The main loop skips a batch slot holding MAX.
+template <int NL, int NB>
+__device__ __forceinline__ void merge_pool(float (&pd)[NL], int (&pi)[NL], const float (&bd)[NB],
+                                           const int (&bi)[NB], bool skip_max, int lane) {
+  constexpr int NC = NL < NB ? NL : NB;
+#pragma unroll
+  for (int m = 0; m < NC; ++m) {
+    const int pr = NL - NC + m, br = NB - NC + m;
+    bool take = pd[pr] > bd[br];
+    if (skip_max && bd[br] == kMaxDist) take = false;
+    if (take) {
+      pd[pr] = bd[br];
+      pi[pr] = bi[br];
+    }
+  }
+  constexpr int L = 32 * NL;
+#pragma unroll
+  for (int sub = L / 2; sub >= 1; sub >>= 1) {
+    if (sub >= 32) {
+      const int rs = sub >> 5;
+#pragma unroll
+      for (int j = 0; j < NL; ++j) {
+        if (j & rs) continue;
+        cx_regs(pd[j], pi[j], pd[j + rs], pi[j + rs], false);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NL; ++j) cx_lanes(pd[j], pi[j], sub, false, lane);
+    }
+  }
+}
+
+// Partial sum of one lane for one row: s = t0*t0, then fmaf(tc, tc, s) over
+// chunks c (t = p - q on dims lane + 32c).  PREC selects the stored format;
+// BF16 and FP8 rows are widened to FP32 before the subtraction.
+template <int C, int PREC>
+struct RowLoader;
+
+template <int C>
+struct RowLoader<C, kPrecF32> {
+  float v[C];
+  __device__ __forceinline__ void load(const SearchArgs& a, int id, int lane) {
+    load_interleaved<C>(a.base + (size_t)id * (32 * C), lane, v);
+  }
+  __device__ __forceinline__ float value(int c) const { return v[c]; }
+};
+
+template <int C>
+struct RowLoader<C, kPrecBF16> {
+  float v[C];
+  __device__ __forceinline__ void load(const SearchArgs& a, int id, int lane) {
+    load_interleaved_bf16<C>(reinterpret_cast<const __nv_bfloat16*>(a.base_bf16) + (size_t)id * (32 * C), lane, v);
+  }
+  __device__ __forceinline__ float value(int c) const { return v[c]; }
+};
+
+template <int C>
+struct RowLoader<C, kPrecFP8> {
+  float v[C];
+  __device__ __forceinline__ void load(const SearchArgs& a, int id, int lane) {
+    float s = __ldg(a.fp8_scale + id);
+    load_interleaved_fp8<C>(a.base_fp8 + (size_t)id * (32 * C), lane, v);
+#pragma unroll
+    for (int c = 0; c < C; ++c) v[c] *= s;
+  }
+  __device__ __forceinline__ float value(int c) const { return v[c]; }
+};
+
+template <int C>
+__device__ __forceinline__ float lane_partial(const float (&p)[C], const float (&q)[C]) {
+  float t = __fsub_rn(p[0], q[0]);
+  float s = __fmul_rn(t, t);
+#pragma unroll
+  for (int c = 1; c < C; ++c) {
+    t = __fsub_rn(p[c], q[c]);
+    s = __fmaf_rn(t, t, s);
+  }
+  return s;
+}
+
+// Distances of the n (<= B) ids in s_ids[0..n) written to s_dist[0..n).
+// Groups of G rows (16, or 8 for long rows): each lane forms its partial for
+// the G rows; a butterfly over offsets 16, 8, ... exchanges half of the rows
+// at each level until every lane holds one row, then plain xor-shuffles
+// finish the sum, which lands in the 32/G lanes lane = t*(32/G) + ...
+// Every addition pairs the same two partial sums as the reference's
+// shuffle-down tree (addition is commutative, so the results are equal).
+template <int C, int PREC>
+__device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)[C],
+                                          const int* s_ids, float* s_dist, int n, int lane) {
+  constexpr int G = C <= 4 ? 16 : 8;
+  constexpr int SPAN = 32 / G;  // lanes sharing one row after the butterfly
+  for (int g0 = 0; g0 < n; g0 += G) {
+    float part[G];
+#pragma unroll
+    for (int t = 0; t < G; ++t) {
+      if (g0 + t < n) {
+        RowLoader<C, PREC> r;
+        r.load(a, s_ids[g0 + t], lane);
+        part[t] = lane_partial<C>(r.v, qv);
+      } else {
+        part[t] = 0.0f;
+      }
+    }
+#pragma unroll
+    for (int off = 16, half = G / 2; half >= 1; off >>= 1, half >>= 1) {
+      const bool up = (lane & off) != 0;
+#pragma unroll
+      for (int t = 0; t < half; ++t) {
+        float send = up ? part[t] : part[t + half];
+        float keep = up ? part[t + half] : part[t];
+        part[t] = __fadd_rn(keep, __shfl_xor_sync(kFull, send, off));
+      }
+    }
+    float total = part[0];
+#pragma unroll
+    for (int off = SPAN / 2; off >= 1; off >>= 1) total = __fadd_rn(total, __shfl_xor_sync(kFull, total, off));
+    const int row = g0 + lane / SPAN;
+    if ((lane % SPAN) == 0 && row < n) s_dist[row] = total;
+  }
+}
+
+// Compact the valid batch ids (0 <= id < np) into s_ids in slot order,
+// compute their distances, and scatter them back (invalid slots -> MAX).
+template <int C, int NB, int PREC>
+__device__ __forceinline__ int batch_distances(const SearchArgs& a, const float (&qv)[C],
+                                               float (&bd)[NB], const int (&bi)[NB], int* s_ids,
+                                               float* s_dist, int lane) {
+  const unsigned lt = (1u << lane) - 1u;
+  int kidx[NB];
+  int n = 0;
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    const bool v = bi[j] >= 0 && bi[j] < a.np;
+    const unsigned m = __ballot_sync(kFull, v);
+    kidx[j] = v ? n + __popc(m & lt) : -1;
+    if (v) s_ids[kidx[j]] = bi[j];
+    n += __popc(m);
+  }
+  __syncwarp();
+  distances<C, PREC>(a, qv, s_ids, s_dist, n, lane);
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < NB; ++j) bd[j] = kidx[j] >= 0 ? s_dist[kidx[j]] : kMaxDist;
+  __syncwarp();
+  return n;
+}
+
+
+// Exact FP32 rerank of the final pool for the reduced-precision paths: the
+// pool ids (visited marks dropped) get FP32 distances computed exactly as
+// the FP32 path computes them, then the pool is bitonic-sorted ascending.
+// The reference's precedent is the host-side parallel_reorder
+// (graph_helper.cu:146-213), which recomputes FP32 L2 and std::sorts.
+template <int C, int NL>
+__device__ __forceinline__ void rerank_pool(const SearchArgs& a, const float (&qv)[C],
+                                            float (&pd)[NL], int (&pi)[NL], int* s_ids,
+                                            float* s_dist, int lane) {
+  const unsigned lt = (1u << lane) - 1u;
+  int kidx[NL];
+  int n = 0;
+#pragma unroll
+  for (int j = 0; j < NL; ++j) {
+    pi[j] = pi[j] < 0 ? -pi[j] : pi[j];
+    const bool v = pi[j] < a.np;
+    const unsigned m = __ballot_sync(kFull, v);
+    kidx[j] = v ? n + __popc(m & lt) : -1;
+    if (v) s_ids[kidx[j]] = pi[j];
+    n += __popc(m);
+  }
+  __syncwarp();
+  distances<C, kPrecF32>(a, qv, s_ids, s_dist, n, lane);
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < NL; ++j) pd[j] = kidx[j] >= 0 ? s_dist[kidx[j]] : kMaxDist;
+  __syncwarp();
+  sort_batch_desc<NL, false>(pd, pi, lane);
+}
+
+template <int C, int NL, int NB, int PREC>
+__device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& bloom, int* s_ids,
+                             float* s_dist) {
+  constexpr int L = 32 * NL;
+  constexpr int B = 32 * NB;
+  const int np = a.np;
+  const int R = a.R;
+  const int NR = R >> 5;  // batch registers per expanded node
+  long long c_entries = 0, c_expanded = 0, c_dists = 0;
+
+  float qv[C];
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const int dim = lane + 32 * c;
+    qv[c] = dim < a.d ? __ldg(a.queries + (size_t)q * a.qstride + dim) : 0.0f;
+  }
+
+  float pd[NL];
+  int pi[NL];
+#pragma unroll
+  for (int j = 0; j < NL; ++j) {
+    pd[j] = kMaxDist;
+    pi[j] = np;
+  }
+  float bd[NB];
+  int bi[NB];
+
+  bloom.clear(lane);
+  __syncwarp();
+
+  // ---- entry phase (graph_search.cuh:479-959) ----
+  int hit = a.entry_mode == 1 ? __ldg(a.hits + q) : 0;
+  if (hit < 0 || hit >= a.n_leaves) hit = 0;
+  const int32_t* lp = a.leaf_pids + (size_t)hit * a.leaf_cap;
+  uint32_t seed0 = (uint32_t)q * 64u + (uint32_t)lane;  // reference thread `lane`
+  uint32_t seed1 = seed0 + 32u;                           // reference thread `lane + 32`
+  constexpr int kEntryBatches = (L + B - 1) / B;
+#pragma unroll 1
+  for (int it = 0; it < kEntryBatches; ++it) {
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      const int pos = it * B + (j << 5) + lane;
+      int id = np;
+      if (pos < L) {
+        if (a.entry_mode == 0) {
+          uint32_t& s = (j & 1) ? seed1 : seed0;
+          s = s * 1103515245u + 12345u;
+          id = (int)(s % (uint32_t)np);
+        } else {
+          id = pos < a.leaf_cap ? __ldg(lp + pos) : np;
+        }
+        bloom.add((uint32_t)id);  // every entry, padding included (:490)
+      }
+      bi[j] = id;
+    }
+    __syncwarp();
+    c_entries += batch_distances<C, NB, PREC>(a, qv, bd, bi, s_ids, s_dist, lane);
+    sort_batch_desc<NB>(bd, bi, lane);
+    merge_pool<NL, NB>(pd, pi, bd, bi, false, lane);
+  }
+
+  // ---- main loop (graph_search.cuh:961-1532) ----
+  uint32_t tmp_flag = 0xFFFFFFFFu;  // (1 << min(L,32)) - 1 with L >= 32 (:969)
+  int iteration = 0;
+  bool cz = false;  // this lane's check_zero (:967)
+  int hash_iteration = 0;
+  int iter = 0;
+
+  auto scan = [&](int chunk) -> uint32_t {  // :1019-1028, :1495-1510
+    bool pred = false;
+    if (chunk < NL) {
+      const int id = pick<NL>(pi, chunk);
+      if (id > 0 && id < np) {
+        pred = true;
+      } else if (id == 0 && !cz) {
+        cz = true;
+        pred = true;
+      }
+    }
+    return __ballot_sync(kFull, pred);
+  };
+
+#pragma unroll 1
+  while (iter < a.max_iter) {
+    iter++;
+    // select up to W unvisited pool slots in pool order; mark them visited by
+    // negating the id (:986-1031)
+    int nodes[NB];
+    int nsel = 0;
+#pragma unroll 1
+    while (nsel < a.W && tmp_flag != 0) {
+      const int pos = __ffs(tmp_flag) - 1;
+      const int chunk = iteration;
+      const int v = __shfl_sync(kFull, pick<NL>(pi, chunk), pos);
+      if (lane == pos) {
+#pragma unroll
+        for (int j = 0; j < NL; ++j)
+          if (j == chunk) pi[j] = -pi[j];
+      }
+      tmp_flag &= ~(1u << pos);
+      const int node = v < 0 ? -v : v;
+#pragma unroll
+      for (int s = 0; s < NB; ++s)
+        if (s == nsel) nodes[s] = node;
+      nsel++;
+      if (nsel == a.W) break;
+      while (tmp_flag == 0 && iteration < NL) {
+        iteration++;
+        tmp_flag = scan(iteration);
+      }
+    }
+    if (nsel == 0) break;
+
+    // neighbour rows of the selected nodes (:995-1010); a node id >= np
+    // expands nothing (the reference would read past the graph)
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      const int s = j / NR;
+      int id = np;
+      if (s < nsel) {
+        const int node = pick<NB>(nodes, s);
+        if (node < np) id = __ldg(a.graph + (size_t)node * R + ((j - s * NR) << 5) + lane);
+      }
+      bi[j] = id;
+    }
+#pragma unroll
+    for (int s = 0; s < NB; ++s) {
+      if (s >= nsel) break;
+      if (lane == 0) c_expanded += pick<NB>(nodes, s) < np ? 1 : 0;
+      // canonical rule: every test of one list sees the filter before any
+      // add of that list; lists in selection order
+      bool pass[NB];
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        pass[j] = false;
+        if (j / NR == s) pass[j] = bi[j] != np && !bloom.test((uint32_t)bi[j]);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        if (j / NR == s) {
+          if (pass[j])
+            bloom.add((uint32_t)bi[j]);
+          else
+            bi[j] = np;
+        }
+      }
+      __syncwarp();
+    }
+
+    c_dists += batch_distances<C, NB, PREC>(a, qv, bd, bi, s_ids, s_dist, lane);
+    sort_batch_desc<NB>(bd, bi, lane);
+    merge_pool<NL, NB>(pd, pi, bd, bi, true, lane);
+
+    bool any = false;
+#pragma unroll 1
+    for (iteration = 0; iteration < NL; iteration++) {
+      tmp_flag = scan(iteration);
+      if (tmp_flag != 0) {
+        any = true;
+        break;
+      }
+    }
+    if (hash_iteration == 4) {  // rebuild from the pool (:1518-1529)
+      __syncwarp();
+      bloom.clear(lane);
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < NL; ++j) {
+        const int id = pi[j] < 0 ? -pi[j] : pi[j];
+        if (id < np) bloom.add((uint32_t)id);
+      }
+      __syncwarp();
+      hash_iteration = 0;
+    }
+    hash_iteration++;
+    if (!any) break;
+  }
+
+  // ---- exact FP32 rerank of the final pool (precision paths) ----
+  if (PREC != kPrecF32 && a.rerank) rerank_pool<C, NL>(a, qv, pd, pi, s_ids, s_dist, lane);
+
+  // ---- output (:1959-1963) ----
+#pragma unroll
+  for (int j = 0; j < NL; ++j) {
+    const int i = (j << 5) + lane;
+    if (i < a.k) {
+      a.out_ids[(size_t)q * a.k + i] = pi[j] < 0 ? -pi[j] : pi[j];
+      if (a.out_dists) a.out_dists[(size_t)q * a.k + i] = pd[j];
+    }
+  }
+  if (a.counters && lane == 0) {
+    long long* c = a.counters + (size_t)q * 4;
+    c[0] = c_entries;
+    c[1] = c_expanded;
+    c[2] = c_dists;
+    c[3] = iter;
+  }
+}
+
+template <int C, int NL, int NB, int PREC>
+__global__ void __launch_bounds__(256, 3) search_kernel(SearchArgs a) {
+  extern __shared__ uint32_t smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  constexpr int B = 32 * NB;
+  constexpr int S = B > 32 * NL ? B : 32 * NL;  // compaction slots per warp
+  const int per_warp = a.bloom_words + 2 * S;
+  uint32_t* wbase = smem + (size_t)wib * per_warp;
+  Bloom bloom;
+  bloom.w = wbase;
+  bloom.words_mask = (uint32_t)a.bloom_words - 1u;
+  bloom.bits_mask = ((uint32_t)a.bloom_words << 5) - 1u;
+  bloom.lw = __ffs(a.bloom_words) - 1;
+  bloom.nh = a.bloom_hashes;
+  int* s_ids = reinterpret_cast<int*>(wbase + a.bloom_words);
+  float* s_dist = reinterpret_cast<float*>(s_ids + S);
+  for (;;) {
+    int q = 0;
+    if (lane == 0) q = (int)atomicAdd(a.work, 1u);
+    q = __shfl_sync(kFull, q, 0);
+    if (q >= a.nq) break;
+    search_query<C, NL, NB, PREC>(a, q, lane, bloom, s_ids, s_dist);
+  }
+}
+
+}  // namespace rte

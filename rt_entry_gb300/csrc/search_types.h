@@ -1,0 +1,27 @@
+// search_types.h -- arguments of the search kernel (host and device).
+#pragma once
+#include <stdint.h>
+
+namespace rte {
+
+enum : int { kPrecF32 = 0, kPrecBF16 = 1, kPrecFP8 = 2 };
+
+struct SearchArgs {
+  const float* base;        // lane-interleaved FP32 rows, stride 32*C floats
+  const uint16_t* base_bf16;  // lane-interleaved BF16 rows (precision 1)
+  const uint8_t* base_fp8;  // lane-interleaved E4M3 rows (precision 2)
+  const float* fp8_scale;   // per-row scale (precision 2)
+  const float* queries;     // row-major [nq][qstride]
+  const int32_t* graph;     // [np][R], padding np
+  const int32_t* leaf_pids; // [n_leaves][leaf_cap], padding np
+  const int32_t* hits;      // [nq] leaf per query
+  int32_t* out_ids;         // [nq][k]
+  float* out_dists;         // [nq][k] or null
+  long long* counters;      // [nq][4] or null
+  unsigned int* work;       // query counter, zero at launch
+  int np, d, qstride, nq, R, W, k, max_iter, bloom_words, bloom_hashes, leaf_cap, entry_mode;
+  int rerank;
+  int n_leaves;             // hits outside [0, n_leaves) fall back to leaf 0
+};
+
+}  // namespace rte

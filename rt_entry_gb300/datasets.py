@@ -1,0 +1,238 @@
+"""Synthetic workloads, exact kNN graphs and FP64 ground truth.
+
+The reference measures on SIFT/DEEP/GIST/COCO files that are not available
+here; seeded synthetic data with their shapes and value ranges stands in.
+Every generator uses numpy's counter-based Philox bit generator with fixed
+seeds (base 1001, queries 2002, training queries 3003, stream 4004).
+
+Graphs: degree-R exact kNN of every base vector (itself excluded), ordered by
+(distance, id).  Ground truth: FP64 brute force, ordered by (distance, id).
+Both run on a CUDA device through torch when one is present (plumbing for
+fixtures, not the measured path) and in numpy otherwise (small sizes).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SEED_BASE, SEED_QUERY, SEED_TRAIN, SEED_STREAM = 1001, 2002, 3003, 4004
+
+
+def _rng(seed):
+    return np.random.Generator(np.random.Philox(seed))
+
+
+@dataclass
+class Mixture:
+    """Isotropic Gaussian mixture: equal weights, per-cluster centres."""
+    centers: np.ndarray
+    sigma: float
+    post: str = "none"          # "none" | "round_clip255" | "unit" | "minmax"
+    lo: np.ndarray | None = field(default=None)
+    hi: np.ndarray | None = field(default=None)
+
+    def sample(self, n: int, seed: int, chunk: int = 1 << 18) -> np.ndarray:
+        rng = _rng(seed)
+        k, d = self.centers.shape
+        out = np.empty((n, d), np.float32)
+        for s in range(0, n, chunk):
+            e = min(n, s + chunk)
+            lab = rng.integers(0, k, e - s)
+            x = self.centers[lab] + np.float32(self.sigma) * rng.standard_normal((e - s, d), np.float32)
+            out[s:e] = self._post(x)
+        return out
+
+    def _post(self, x):
+        if self.post == "round_clip255":
+            return np.rint(np.clip(x, 0, 255)).astype(np.float32)
+        if self.post == "unit":
+            nrm = np.linalg.norm(x, axis=1, keepdims=True)
+            return (x / np.maximum(nrm, 1e-12)).astype(np.float32)
+        if self.post == "minmax":
+            return ((x - self.lo) / (self.hi - self.lo)).astype(np.float32)
+        return x.astype(np.float32)
+
+
+@dataclass
+class Workload:
+    name: str
+    base: np.ndarray
+    queries: np.ndarray
+    degree: int
+    leaf_size: int = 32
+    expand_ratio: float = 0.2
+    k: int = 10
+    beam: int = 64
+    mixture: Mixture | None = None
+    graph: np.ndarray | None = None
+    gt: np.ndarray | None = None
+
+
+def mixture_config(cfg: int, d: int | None = None) -> Mixture:
+    """Mixture of configuration `cfg` (1..4)."""
+    rng = _rng(SEED_BASE + 17 * cfg)
+    if cfg == 1:   # 64 components, centres U[0,100]^d, sigma 5
+        d = d or 128
+        return Mixture(rng.uniform(0, 100, (64, d)).astype(np.float32), 5.0)
+    if cfg == 2:   # 256 clusters, integer values 0..255 (SIFT-like bvecs)
+        d = d or 128
+        return Mixture(rng.uniform(32, 224, (256, d)).astype(np.float32), 64.0, "round_clip255")
+    if cfg == 3:   # 128 clusters, N(0,1) per dim around N(0,1) centres, min-max to [0,1]
+        d = d or 960
+        return Mixture(rng.standard_normal((128, d), np.float32), 1.0, "minmax")
+    if cfg == 4:   # 1024 clusters on the unit sphere (angular, DEEP-like)
+        d = d or 96
+        return Mixture(rng.standard_normal((1024, d), np.float32), 0.35, "unit")
+    raise ValueError(cfg)
+
+
+def make_config(cfg: int, n: int | None = None, nq: int | None = None, d: int | None = None,
+                with_graph: bool = True, with_gt: bool = True, gt_k: int = 100,
+                device: str | None = None) -> Workload:
+    """Config 1..4 at its published size (or the given n / nq / d)."""
+    sizes = {1: (100_000, 10_000, 32), 2: (1_000_000, 10_000, 64), 3: (1_000_000, 1_000, 64),
+             4: (10_000_000, 10_000, 32)}
+    n0, nq0, R = sizes[cfg]
+    n = n or n0
+    nq = nq or nq0
+    mix = mixture_config(cfg, d)
+    if mix.post == "minmax":
+        raw = Mixture(mix.centers, mix.sigma).sample(n, SEED_BASE)
+        mix.lo = raw.min(axis=0)
+        mix.hi = np.maximum(raw.max(axis=0), mix.lo + 1e-6)
+        base = mix._post(raw)
+        q = mix._post(Mixture(mix.centers, mix.sigma).sample(nq, SEED_QUERY))
+    else:
+        base = mix.sample(n, SEED_BASE)
+        q = mix.sample(nq, SEED_QUERY)
+    w = Workload(f"config{cfg}", base, q, R, mixture=mix)
+    if with_graph:
+        w.graph = knn_graph(base, R, device=device)
+    if with_gt:
+        w.gt = ground_truth(base, q, min(gt_k, n), device=device)
+    return w
+
+
+def _torch_device(device):
+    try:
+        import torch
+    except ImportError:
+        return None, None
+    if device is None:
+        device = "cuda" if torch.cuda.is_available() else None
+    if device is None:
+        return torch, None
+    return torch, torch.device(device)
+
+
+def _sort_by_dist_then_id(d, i):
+    """Rows of (dist, id) candidates -> lexicographic order (numpy)."""
+    o = np.lexsort((i, d), axis=-1)
+    return np.take_along_axis(d, o, -1), np.take_along_axis(i, o, -1)
+
+
+def knn_graph(base: np.ndarray, R: int, device: str | None = None, chunk: int = 4096) -> np.ndarray:
+    """Exact degree-R kNN graph (self excluded), rows ordered by (dist, id)."""
+    n = base.shape[0]
+    if n <= R:
+        raise ValueError("need more than R base vectors")
+    torch, dev = _torch_device(device)
+    extra = 8
+    out = np.empty((n, R), np.int32)
+    if dev is not None:
+        prev = torch.backends.cuda.matmul.allow_tf32
+        torch.backends.cuda.matmul.allow_tf32 = False
+        try:
+            X = torch.from_numpy(base).to(dev)
+            nrm = (X.double() ** 2).sum(1).float()
+            for s in range(0, n, chunk):
+                e = min(n, s + chunk)
+                D = nrm[s:e, None] + nrm[None, :] - 2.0 * (X[s:e] @ X.T)
+                D[torch.arange(e - s, device=dev), torch.arange(s, e, device=dev)] = float("inf")
+                dv, iv = torch.topk(D, R + extra, dim=1, largest=False)
+                # exact FP64 distances of the candidates, then (dist, id) order
+                cand = X[iv.reshape(-1)].reshape(e - s, R + extra, -1).double()
+                dd = ((cand - X[s:e, None, :].double()) ** 2).sum(-1)
+                dd_np, iv_np = _sort_by_dist_then_id(dd.cpu().numpy(), iv.cpu().numpy())
+                out[s:e] = iv_np[:, :R]
+        finally:
+            torch.backends.cuda.matmul.allow_tf32 = prev
+        return out
+    X = base.astype(np.float64)
+    nrm = (X ** 2).sum(1)
+    for s in range(0, n, 1024):
+        e = min(n, s + 1024)
+        D = nrm[s:e, None] + nrm[None, :] - 2.0 * (X[s:e] @ X.T)
+        D[np.arange(e - s), np.arange(s, e)] = np.inf
+        iv = np.argpartition(D, R + extra, axis=1)[:, :R + extra]
+        cand = X[iv]
+        dd = ((cand - X[s:e, None, :]) ** 2).sum(-1)
+        _, iv = _sort_by_dist_then_id(dd, iv)
+        out[s:e] = iv[:, :R]
+    return out
+
+
+def ground_truth(base: np.ndarray, queries: np.ndarray, k: int = 100, device: str | None = None,
+                 chunk: int = 1024) -> np.ndarray:
+    """FP64 brute-force k nearest base ids per query, ordered by (dist, id)."""
+    torch, dev = _torch_device(device)
+    nq = queries.shape[0]
+    out = np.empty((nq, k), np.int32)
+    extra = 16
+    kk = min(base.shape[0], k + extra)
+    if dev is not None:
+        X = torch.from_numpy(base).to(dev).double()
+        nrm = (X ** 2).sum(1)
+        Q = torch.from_numpy(queries).to(dev).double()
+        for s in range(0, nq, chunk):
+            e = min(nq, s + chunk)
+            q = Q[s:e]
+            D = (q ** 2).sum(1)[:, None] + nrm[None, :] - 2.0 * (q @ X.T)
+            _, iv = torch.topk(D, kk, dim=1, largest=False)
+            cand = X[iv.reshape(-1)].reshape(e - s, kk, -1)
+            dd = ((cand - q[:, None, :]) ** 2).sum(-1)
+            _, iv_np = _sort_by_dist_then_id(dd.cpu().numpy(), iv.cpu().numpy())
+            out[s:e] = iv_np[:, :k]
+        return out
+    X = base.astype(np.float64)
+    nrm = (X ** 2).sum(1)
+    for s in range(0, nq, 256):
+        e = min(nq, s + 256)
+        q = queries[s:e].astype(np.float64)
+        D = (q ** 2).sum(1)[:, None] + nrm[None, :] - 2.0 * (q @ X.T)
+        iv = np.argpartition(D, kk - 1, axis=1)[:, :kk] if kk < base.shape[0] else np.tile(
+            np.arange(base.shape[0]), (e - s, 1))
+        dd = ((X[iv] - q[:, None, :]) ** 2).sum(-1)
+        _, iv = _sort_by_dist_then_id(dd, iv)
+        out[s:e] = iv[:, :k]
+    return out
+
+
+def recall_at(ids: np.ndarray, gt: np.ndarray, k: int = 10) -> float:
+    """k@k recall: fraction of the true top-k found among the returned top-k."""
+    ids = np.asarray(ids)[:, :k]
+    gt = np.asarray(gt)[:, :k]
+    hit = 0
+    for a, b in zip(ids, gt):
+        hit += len(np.intersect1d(a, b, assume_unique=False))
+    return hit / (gt.shape[0] * k)
+
+
+def recall_reference_style(ids: np.ndarray, gt: np.ndarray, k: int = 10) -> float:
+    """The reference's recall@k: true top-k ids found anywhere in the returned
+    list (graph_helper.cu:64-80), which with topk = beam is k@beam."""
+    hit = 0
+    for a, b in zip(np.asarray(ids), np.asarray(gt)[:, :k]):
+        hit += np.isin(b, a).sum()
+    return hit / (gt.shape[0] * k)
+
+
+def stream_batches(n_batches: int = 2000, max_batch: int = 8192, seed: int = SEED_STREAM):
+    """Config-5 batch plan: sizes floor(exp(U[0, ln max_batch])), k in {1,10,100}."""
+    rng = _rng(seed)
+    sizes = np.floor(np.exp(rng.uniform(0, math.log(max_batch), n_batches))).astype(np.int64)
+    sizes = np.maximum(sizes, 1)
+    ks = rng.choice(np.array([1, 10, 100]), n_batches)
+    return sizes, ks

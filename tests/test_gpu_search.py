@@ -1,0 +1,246 @@
+"""GPU parity: the CUDA query path against the oracle and the reference's
+own kernel, through the C ABI.
+
+Bars: ids bit-exact and distances bit-exact against the oracle (the kernel
+and the oracle run the same FP32 operations in the same order); the
+reference kernel returns ids only, so against it ids are compared; PCA and
+projection within FP64 tolerances stated per test.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = os.path.join(ROOT, "tests", "golden")
+sys.path.insert(0, GOLD)
+import make_search_golden as golden  # noqa: E402
+
+
+def _index(base, graph, leaf=32, expand=0.2, pca=False):
+    import rt_entry_gb300 as r
+    idx = r.Index.from_arrays(base, graph)
+    if pca:
+        idx.build_pca()
+    idx.build_kdtree(leaf, expand)
+    return idx
+
+
+def _mixture(n, nq, d, integer, seed, k=12, spread=45.0):
+    rng = np.random.Generator(np.random.Philox(seed))
+    cent = rng.uniform(40, 215, (k, d))
+    x = cent[rng.integers(0, k, n + nq)] + spread * rng.standard_normal((n + nq, d))
+    x = np.clip(x, 0, 255)
+    x = np.rint(x) if integer else x
+    x = x.astype(np.float32)
+    return x[:n], x[n:]
+
+
+@pytest.mark.parametrize("case", [c[0] for c in golden.CASES])
+def test_search_matches_reference_kernel_and_oracle(lib, orc, cuda, case):
+    c = golden.load_case(case)
+    L = int(c["beam"])
+    idx = _index(c["base"], c["graph"], int(c["leaf"]), float(c["expand_ratio"]))
+    _, _, pids = idx.kdtree()
+    assert np.array_equal(pids, c["leaf_pids"])
+    hits = idx.locate(c["queries"])
+    assert np.array_equal(hits, c["hits"])
+    ids, d = idx.search_projected(c["queries"], beam=L, k=L, max_iter=int(c["max_iter"]),
+                                  entry_mode=int(c["algo"]))
+    oids, od = orc.search(c["base"], c["queries"], c["graph"], L=L, k=L,
+                          max_iter=int(c["max_iter"]), entry_mode=int(c["algo"]),
+                          leaf_pids=c["leaf_pids"], hits=c["hits"])
+    assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ from the oracle"
+    assert np.array_equal(d, od)
+    if "ref_ids" in c:
+        assert np.array_equal(ids, c["ref_ids"]), "differs from the reference kernel"
+
+
+SWEEP = [
+    # d, integer, degree, beam, width, bloom words, hashes, entry mode, max_iter
+    (32, True, 32, 32, 1, 512, 3, 1, 100),
+    (64, False, 64, 64, 1, 512, 3, 1, 100),
+    (96, True, 32, 128, 2, 512, 3, 1, 100),
+    (128, True, 64, 64, 1, 2048, 3, 1, 100),
+    (128, False, 64, 128, 2, 4096, 2, 1, 60),
+    (128, True, 32, 256, 4, 8192, 3, 1, 100),
+    (96, False, 32, 64, 1, 512, 3, 0, 100),
+    (128, True, 64, 32, 1, 32, 5, 1, 100),      # tiny filter: many false positives
+    (128, False, 64, 64, 1, 512, 3, 1, 7),      # stops at max_iter
+    (128, True, 32, 64, 2, 1024, 1, 0, 100),
+]
+
+
+@pytest.mark.parametrize("d,integer,R,L,W,bw,nh,mode,mi", SWEEP)
+def test_search_matches_oracle_sweep(lib, orc, cuda, d, integer, R, L, W, bw, nh, mode, mi):
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(3000, 300, d, integer, seed=d * 1000 + L + W + bw + mode + mi)
+    graph = ds.knn_graph(base, R)
+    idx = _index(base, graph, 24, 0.2)
+    _, _, pids = idx.kdtree()
+    hits = idx.locate(q)
+    kw = dict(beam=L, k=L, search_width=W, bloom_words=bw, bloom_hashes=nh, entry_mode=mode,
+              max_iter=mi)
+    ids, dd = idx.search_projected(q, **kw)
+    oids, od, ocnt = orc.search(base, q, graph, L=L, k=L, search_width=W, bloom_words=bw,
+                                bloom_hashes=nh, entry_mode=mode, max_iter=mi, leaf_pids=pids,
+                                hits=hits, with_counters=True)
+    assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
+    assert np.array_equal(dd, od)
+    cnt = idx.counters(q, **kw)
+    assert np.array_equal(cnt, ocnt)
+    # run twice: bytes identical
+    ids2, dd2 = idx.search_projected(q, **kw)
+    assert np.array_equal(ids, ids2) and np.array_equal(dd, dd2)
+
+
+def test_topk_prefix_and_host_device_io(lib, orc, cuda):
+    import torch
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(2500, 200, 128, True, seed=77)
+    graph = ds.knn_graph(base, 64)
+    idx = _index(base, graph, 32, 0.2)
+    full, fd = idx.search_projected(q, beam=64, k=64)
+    top, td = idx.search_projected(q, beam=64, k=10)
+    assert np.array_equal(top, full[:, :10]) and np.array_equal(td, fd[:, :10])
+    # device tensors in, device tensors out; same bytes
+    qt = torch.from_numpy(q).cuda()
+    it, dt = idx.search_projected(qt, beam=64, k=10)
+    assert it.is_cuda and np.array_equal(it.cpu().numpy(), top)
+    s = torch.cuda.Stream()
+    it2, _ = idx.search_projected(qt, beam=64, k=10, stream=s)
+    s.synchronize()
+    assert np.array_equal(it2.cpu().numpy(), top)
+
+
+def test_pca_against_fp64_and_reference_golden(lib, cuda):
+    import rt_entry_gb300 as r
+    z = np.load(os.path.join(GOLD, "pca_ref.npz"))
+    x = z["x"].astype(np.float32)
+    g = np.zeros((x.shape[0], 32), np.int32)
+    idx = r.Index.from_arrays(x, g).build_pca()
+    mean, rot, ev = idx.pca()
+    assert np.allclose(mean, z["mean"], rtol=0, atol=1e-4)
+    assert np.allclose(ev, z["eigvals"], rtol=1e-9, atol=1e-9 * ev[0])
+    ref = z["eigvecs"]
+    sign = np.sign((ref * rot).sum(0))
+    sep = np.minimum(np.abs(np.diff(ev, prepend=np.inf)), np.abs(np.diff(ev, append=-np.inf)))
+    ok = sep > 1e-6 * ev[0]
+    assert np.abs(ref[:, ok] * sign[ok] - rot[:, ok]).max() < 1e-6
+    # projected base vs the reference's (Eigen FP64, rounded to float)
+    pb = idx.search_base()
+    refp = z["projected"] * sign[None, :]
+    scale = np.abs(refp).max()
+    assert np.abs(pb[:, ok] - refp[:, ok]).max() <= 1e-5 * scale
+    # query projection vs FP64
+    q = x[:500] + 0.5
+    qp = idx.project(q)
+    exact = (q.astype(np.float64) - z["mean"]) @ rot.astype(np.float64)
+    assert np.abs(qp - exact).max() <= 1e-5 * np.abs(exact).max()
+
+
+def test_pca_keep_dims_and_kdtree_consistency(lib, orc, cuda):
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(4000, 100, 96, False, seed=5)
+    graph = ds.knn_graph(base, 32)
+    idx = r.Index.from_arrays(base, graph).build_pca(keep_dims=64).build_kdtree(32, 0.2)
+    assert idx.info.search_dim == 64
+    pb = idx.search_base()
+    t, e, p = idx.kdtree()
+    b, pp = orc.kdtree_build(pb[:, :3], 32)
+    assert np.array_equal(t, b) and np.array_equal(p, pp)
+    assert np.array_equal(e, orc.expand_boxes(b, 0.2))
+    qp = idx.project(q)
+    assert qp.shape == (100, 64)
+    ids, dd = idx.search(q, beam=64, k=64)
+    oids, od = orc.search(pb, qp, graph, L=64, k=64, leaf_pids=p, hits=orc.locate(e, qp))
+    assert np.array_equal(ids, oids) and np.array_equal(dd, od)
+
+
+def test_locate_matches_oracle_including_faces(lib, orc, cuda):
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base, _ = _mixture(5000, 1, 32, False, seed=9)
+    idx = _index(base, ds.knn_graph(base, 32), 16, 0.2)
+    t, e, p = idx.kdtree()
+    rng = np.random.default_rng(0)
+    lo, hi = e[:, :3].min(0), e[:, 3:].max(0)
+    pts = np.zeros((20000, 32), np.float32)
+    pts[:, :3] = rng.uniform(lo - 5, hi + 5, (20000, 3))
+    # points exactly on box faces and corners
+    pick = rng.integers(0, e.shape[0], 3000)
+    pts[:3000, 0] = e[pick, 0]
+    pts[3000:6000, 1] = e[pick, 4]
+    pts[6000:9000, :3] = e[pick, 3:6]
+    got = idx.locate(pts)
+    want = orc.locate(e, pts)
+    assert np.array_equal(got, want)
+    assert (want == 0).any()  # misses fall back to leaf 0
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+@pytest.mark.parametrize("rerank", [0, 1])
+def test_low_precision_paths_match_oracle(lib, orc, cuda, prec, rerank):
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(3000, 200, 128, False, seed=31 + prec)
+    graph = ds.knn_graph(base, 64)
+    idx = _index(base, graph, 32, 0.2)
+    _, _, pids = idx.kdtree()
+    hits = idx.locate(q)
+    low = idx.search_base_lowp(prec)
+    if prec == 1:
+        bits = base.view(np.uint32).astype(np.uint64)
+        rne = ((bits + 0x7FFF + ((bits >> 16) & 1)) >> 16 << 16).astype(np.uint32)
+        assert np.array_equal(low, rne.view(np.float32))
+    else:
+        rel = np.abs(low - base) / np.maximum(np.abs(base).max(1, keepdims=True), 1e-9)
+        assert rel.max() <= 2 ** -4 + 1e-6  # E4M3: 3 mantissa bits, scale = max|x|/448
+    ids, dd = idx.search_projected(q, beam=64, k=64, precision=prec, rerank=rerank)
+    oids, od = orc.search(low, q, graph, L=64, k=64, leaf_pids=pids, hits=hits,
+                          rerank_base=base if rerank else None)
+    assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
+    assert np.array_equal(dd, od)
+
+
+def test_parameter_errors(lib, cuda):
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(1000, 10, 32, True, seed=3)
+    idx = r.Index.from_arrays(base, ds.knn_graph(base, 32))
+    with pytest.raises(r.RteError) as e:
+        idx.search_projected(q, beam=64, k=10)  # kd-tree entries before the kd-tree
+    assert e.value.status == r.RTE_ESTATE
+    idx.build_kdtree(32, 0.2)
+    for kw in (dict(beam=64, k=65), dict(beam=16, k=10), dict(beam=512, k=10),
+               dict(beam=64, k=10, bloom_words=1000), dict(beam=64, k=10, bloom_hashes=11),
+               dict(beam=64, k=10, search_width=3), dict(beam=64, k=10, precision=7),
+               dict(beam=64, k=10, max_iter=-1)):
+        with pytest.raises(r.RteError) as e:
+            idx.search_projected(q, **kw)
+        assert e.value.status == r.RTE_EINVAL, kw
+    # empty batch is fine
+    ids, dd = idx.search_projected(q[:0], beam=64, k=10)
+    assert ids.shape == (0, 10)
+    # out-of-range caller hits fall back to leaf 0 instead of reading out of bounds
+    bad = np.full(len(q), 10 ** 6, np.int32)
+    ids1, _ = idx.search_projected(q, hits=bad, beam=64, k=10)
+    ids0, _ = idx.search_projected(q, hits=np.zeros(len(q), np.int32), beam=64, k=10)
+    assert np.array_equal(ids1, ids0)
+
+
+def test_save_load_roundtrip(lib, cuda, tmp_path):
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(3000, 100, 64, True, seed=12)
+    graph = ds.knn_graph(base, 32)
+    idx = r.Index.from_arrays(base, graph).build_pca().build_kdtree(32, 0.2)
+    ids, dd = idx.search(q, beam=64, k=10)
+    idx.save(str(tmp_path / "ix"))
+    assert (tmp_path / "ix" / "32_0.aabbs").exists() and (tmp_path / "ix" / "O.fbin").exists()
+    idx2 = r.Index.load_dir(str(tmp_path / "ix"))
+    ids2, dd2 = idx2.search(q, beam=64, k=10)
+    assert np.array_equal(ids, ids2) and np.array_equal(dd, dd2)

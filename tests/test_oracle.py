@@ -1,0 +1,98 @@
+"""The oracle (CPU restatement) against the reference's own outputs."""
+import os
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = os.path.join(ROOT, "tests", "golden")
+
+
+def test_kdtree_oracle_matches_reference(orc):
+    z = np.load(os.path.join(GOLD, "kdtree_ref.npz"))
+    for n in sorted(set(k.split("__")[0] for k in z.files)):
+        b, p = orc.kdtree_build(z[n + "__pts"], int(z[n + "__cap"]))
+        assert np.array_equal(b, z[n + "__boxes"]), n
+        assert np.array_equal(p, z[n + "__pids"]), n
+
+
+def _cases():
+    import sys
+    sys.path.insert(0, GOLD)
+    import make_search_golden as g
+    return g
+
+
+@pytest.mark.parametrize("case", [c[0] for c in _cases().CASES])
+def test_search_oracle_matches_reference_kernel(orc, case):
+    """Ids of the whole final pool equal the reference GraphSearchKernel's,
+    run on a GB300 from a cubin compiled from graph_search.cuh."""
+    g = _cases()
+    c = g.load_case(case)
+    if "ref_ids" not in c:
+        pytest.skip("fixture has no reference ids yet")
+    L = int(c["beam"])
+    ids, dists = orc.search(c["base"], c["queries"], c["graph"], L=L, k=L,
+                            max_iter=int(c["max_iter"]), entry_mode=int(c["algo"]),
+                            leaf_pids=c["leaf_pids"], hits=c["hits"])
+    ref = c["ref_ids"]
+    assert ids.shape == ref.shape
+    mism = (ids != ref).any(axis=1)
+    assert not mism.any(), f"{mism.sum()} of {len(mism)} queries differ"
+
+
+def test_search_golden_inputs_are_consistent(orc):
+    """The stored leaf table and hits are what the oracle computes."""
+    g = _cases()
+    for case, *_ in g.CASES:
+        c = g.load_case(case)
+        b, p = orc.kdtree_build(c["base"][:, :3], int(c["leaf"]))
+        assert np.array_equal(p, c["leaf_pids"])
+        h = orc.locate(orc.expand_boxes(b, float(c["expand_ratio"])), c["queries"][:, :3])
+        assert np.array_equal(h, c["hits"])
+
+
+def test_oracle_pool_is_sorted_and_valid(orc):
+    g = _cases()
+    c = g.load_case("int_d32_r32_l64")
+    ids, d, cnt = orc.search(c["base"], c["queries"], c["graph"], L=64, k=64,
+                             leaf_pids=c["leaf_pids"], hits=c["hits"], with_counters=True)
+    assert (np.diff(d, axis=1) >= 0).all()
+    n = c["base"].shape[0]
+    assert ((ids >= 0) & (ids <= n)).all()
+    # distances are the reference's arithmetic on the returned ids
+    for qi in range(5):
+        for j in range(0, 64, 9):
+            if ids[qi, j] < n:
+                assert d[qi, j] == orc.l2_ref(c["base"][ids[qi, j]], c["queries"][qi])
+    assert (cnt[:, 0] > 0).all() and (cnt[:, 3] <= 100).all()
+
+
+def test_oracle_l2_matches_fp64_closely(orc):
+    rng = np.random.default_rng(0)
+    for d in (1, 31, 32, 33, 96, 128, 960):
+        p = rng.standard_normal(d).astype(np.float32)
+        q = rng.standard_normal(d).astype(np.float32)
+        exact = float(((p.astype(np.float64) - q) ** 2).sum())
+        assert abs(orc.l2_ref(p, q) - exact) <= 1e-5 * exact
+
+
+def test_oracle_recall_on_small_mixture(orc):
+    from rt_entry_gb300 import datasets as ds
+    mix = ds.mixture_config(1, 32)
+    base = mix.sample(3000, ds.SEED_BASE)
+    q = mix.sample(100, ds.SEED_QUERY)
+    g = ds.knn_graph(base, 32, device="cpu")
+    gt = ds.ground_truth(base, q, 10, device="cpu")
+    b, p = orc.kdtree_build(base[:, :3], 32)
+    hits = orc.locate(orc.expand_boxes(b, 0.2), q[:, :3])
+    ids, _ = orc.search(base, q, g, L=64, k=10, leaf_pids=p, hits=hits)
+    assert ds.recall_at(ids, gt, 10) > 0.9
+
+
+def test_oracle_rejects_bad_arguments(orc):
+    base = np.zeros((10, 4), np.float32)
+    with pytest.raises(ValueError):
+        orc.search(base, base, np.zeros((10, 24), np.int32), L=32, k=10, entry_mode=0)
+    with pytest.raises(ValueError):
+        orc.search(base, base, np.zeros((10, 32), np.int32), L=32, k=64, entry_mode=0)
