@@ -184,6 +184,58 @@ rte_status rte_kdtree_build_host(const float* xyz, int64_t n, int leaf_size, flo
  * column j, largest-magnitude component positive. */
 rte_status rte_sym_eig_host(const double* a, int n, double* w, double* v);
 
+/* ---- learned entry (no reference counterpart; spec form 4) ----
+ * A 3-layer MLP (search-space query -> hidden -> hidden -> kd-tree leaf)
+ * proposes each query's entry leaf.  With RTE_ENTRY_LEARNED the entry list
+ * is the proposed leaf's points followed by the kd-tree leaf's points (the
+ * kd-tree stays the fallback), truncated to the beam. */
+typedef struct {
+  int hidden;      /* hidden width, multiple of 8 (256)                       */
+  int epochs;      /* passes over the training queries (4)                    */
+  int batch;       /* rows per step, multiple of 128 (4096)                   */
+  float lr;        /* Adam learning rate, cosine-decayed to lr/10 (2e-3)      */
+  int label_beam;  /* beam of the plain search that labels the queries (64)   */
+  int seed;        /* initialisation and shuffling seed (3003)                */
+} rte_train_params;
+
+typedef struct {
+  float first_loss, last_loss; /* mean cross-entropy of the first / last batch */
+  float train_acc;             /* top-1 leaf accuracy on one training batch    */
+  int64_t n_train;
+  int classes;                 /* output width = kd-tree leaves                */
+  int64_t steps;
+  float train_ms;              /* device time of the optimisation loop         */
+} rte_train_report;
+
+void rte_default_train_params(rte_train_params* p);
+/* Labels every training query with the leaf holding the best result of the
+ * plain kd-tree search (beam label_beam), then trains the MLP on the GPU
+ * with BF16 tensor-core GEMMs (FP32 accumulation), softmax cross-entropy
+ * and Adam.  Requires the kd-tree; at most 65536 leaves. */
+rte_status rte_learned_train(rte_index* idx, const float* train_queries, int64_t n,
+                             const rte_train_params* params, rte_train_report* report);
+/* The MLP's leaf for each projected query [nq x search_dim]. */
+rte_status rte_learned_predict(rte_index* idx, const float* projected, int64_t nq,
+                               int32_t* out_leaf, void* stream);
+
+/* One forward + backward pass of the learned-entry MLP on given FP32
+ * inputs and weights (rounded to BF16 as training does), for checking the
+ * GPU gradients against a CPU restatement.  X [M x d], labels [M], W1
+ * [hidden x d], W2 [hidden x hidden], W3 [classes x hidden]; gradients of
+ * the mean cross-entropy in the same shapes, per-row loss [M] (may be NULL). */
+rte_status rte_mlp_grad_check(const float* X, const int32_t* labels, int M, int d, int hidden,
+                              int classes, const float* W1, const float* b1, const float* W2,
+                              const float* b2, const float* W3, const float* b3, float* gW1,
+                              float* gb1, float* gW2, float* gb2, float* gW3, float* gb3,
+                              float* loss);
+
+/* BF16 tensor-core GEMM of the learned-entry MLP (tcgen05 + TMA + TMEM):
+ * C [M x N] FP32 = A [M x K] * B [N x K]^T, A and B BF16 bit patterns,
+ * row-major, K a multiple of 8.  Host or device pointers.  RTE_ETIMEOUT if
+ * a bounded pipeline wait ran out.  (No reference counterpart.) */
+rte_status rte_gemm_bf16(const uint16_t* A, const uint16_t* B, int M, int N, int K, float* C,
+                         void* stream);
+
 /* Message of the last failure on this thread ("" if none). */
 const char* rte_last_error(void);
 

@@ -92,8 +92,8 @@ def lib():
         L.orc_search.argtypes = [P, i64, i32, P, i64, P, i32, P, i32, P, i32, i32, i32, i32, i32,
                                  i32, i32, P, P, P, i32]
         L.orc_search.restype = i32
-        L.orc_search_rerank.argtypes = [P, P, i64, i32, P, i64, P, i32, P, i32, P, i32, i32, i32,
-                                        i32, i32, i32, i32, P, P, P, i32]
+        L.orc_search_rerank.argtypes = [P, P, i64, i32, P, i64, P, i32, P, i32, P, P, i32, i32,
+                                        i32, i32, i32, i32, i32, P, P, P, i32]
         L.orc_search_rerank.restype = i32
         L.orc_l2_ref.argtypes = [P, P, i32]
         L.orc_l2_ref.restype = f32
@@ -119,7 +119,7 @@ def _c(a, dt):
 
 def search(base, queries, graph, *, L, k, search_width=1, max_iter=100, bloom_words=512,
            bloom_hashes=3, entry_mode=1, leaf_pids=None, hits=None, n_threads=0,
-           with_counters=False, rerank_base=None):
+           with_counters=False, rerank_base=None, hits2=None):
     """Restated GraphSearchKernel over (base, queries, graph) -> (ids, dists[, counters]).
 
     With rerank_base, `base` is the reduced-precision copy (as FP32) the
@@ -136,8 +136,9 @@ def search(base, queries, graph, *, L, k, search_width=1, max_iter=100, bloom_wo
     cnt = (Counters * max(nq, 1))() if with_counters else None
     lp = None if leaf_pids is None else _c(leaf_pids, np.int32)
     h = None if hits is None else _c(hits, np.int32)
+    h2 = None if hits2 is None else _c(hits2, np.int32)
     cap = 0 if lp is None else lp.shape[1]
-    rc = lib().orc_search_rerank(_p(base), _p(rb), np_, d, _p(queries), nq, _p(graph), degree, _p(lp), cap, _p(h),
+    rc = lib().orc_search_rerank(_p(base), _p(rb), np_, d, _p(queries), nq, _p(graph), degree, _p(lp), cap, _p(h), _p(h2),
                           L, k, search_width, max_iter, bloom_words, bloom_hashes, entry_mode,
                           _p(ids), _p(dists), None if cnt is None else ctypes.cast(cnt, ctypes.c_void_p),
                           n_threads)

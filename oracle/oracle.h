@@ -56,8 +56,8 @@ int orc_search(const float* base, int64_t np, int d, const float* queries, int64
  * then the reduced-precision copy the search ran on (dequantized to FP32). */
 int orc_search_rerank(const float* base, const float* rerank_base, int64_t np, int d,
                       const float* queries, int64_t nq, const int32_t* graph, int degree,
-                      const int32_t* leaf_pids, int leaf_cap, const int32_t* hits, int L, int k,
-                      int search_width, int max_iter, int bloom_words, int bloom_hashes,
+                      const int32_t* leaf_pids, int leaf_cap, const int32_t* hits,
+                      const int32_t* hits2, int L, int k, int search_width, int max_iter, int bloom_words, int bloom_hashes,
                       int entry_mode, int32_t* out_ids, float* out_dists, orc_counters* counters,
                       int n_threads);
 

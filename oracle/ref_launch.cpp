@@ -9,6 +9,12 @@
 // Safe-launch conditions (checked below): search_width == 1 (the reference's
 // first selection mask is all ones, so a wider first expansion can reach an
 // empty slot whose id np indexes one row past the graph); degree <= 64.
+//
+// scrub != 0: one launch per query (grid 1, pointers offset to that query),
+// each preceded by scrub_smem (oracle/ref/scrub.cu) on every SM, so that the
+// reference's never-cleared shared bloom filter (graph_search.cuh:88) starts
+// empty.  Only meaningful for kd-tree entries: random entries seed from
+// blockIdx.x (graph_search.cuh:64), which a per-query launch changes.
 #include <cuda.h>
 
 #include <cstdint>
@@ -47,7 +53,7 @@ extern "C" int ref_graph_search(const char* cubin_path, const float* data, int n
                                 const float* queries, int nq, const int* graph, int degree,
                                 const int* entries, int n_leaves, int n_candidates,
                                 const int* hits, int topk, int search_width, int max_iter, int algo,
-                                int* out) {
+                                int scrub, int* out) {
   if (search_width != 1 || degree > 64 || degree <= 0 || (degree & (degree - 1)) || topk <= 0 ||
       topk > n_candidates || nq <= 0 || np <= 0 || n_leaves <= 0) {
     g_msg = "rejected arguments (search_width must be 1, degree a power of two <= 64)";
@@ -108,8 +114,41 @@ extern "C" int ref_graph_search(const char* cubin_path, const float* data, int n
                     &np,       &offset_shift, &n_candidates, &topk,         &search_width,
                     &d_entries.p, &d_hits.p, &max_iter,    &algo};
     const unsigned smem = (unsigned)(((search_width << offset_shift) + n_candidates) * 8);
-    DRV(cuLaunchKernel(fn, nq, 1, 1, 64, 1, 1, smem, nullptr, args, nullptr));
-    DRV(cuCtxSynchronize());
+    if (!scrub) {
+      DRV(cuLaunchKernel(fn, nq, 1, 1, 64, 1, 1, smem, nullptr, args, nullptr));
+      DRV(cuCtxSynchronize());
+    } else {
+      std::string dir(cubin_path);
+      dir = dir.substr(0, dir.find_last_of('/') + 1);
+      CUmodule smod;
+      if (cuModuleLoad(&smod, (dir + "scrub.cubin").c_str()) != CUDA_SUCCESS) {
+        g_msg = "cannot load scrub.cubin";
+        cuModuleUnload(mod);
+        cuCtxPopCurrent(&ctx);
+        return -2;
+      }
+      CUfunction sf;
+      DRV(cuModuleGetFunction(&sf, smod, "scrub_smem"));
+      int max_smem = 0, nsm = 0;
+      DRV(cuDeviceGetAttribute(&max_smem, CU_DEVICE_ATTRIBUTE_MAX_SHARED_MEMORY_PER_BLOCK_OPTIN, dev));
+      DRV(cuDeviceGetAttribute(&nsm, CU_DEVICE_ATTRIBUTE_MULTIPROCESSOR_COUNT, dev));
+      DRV(cuFuncSetAttribute(sf, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, max_smem));
+      DRV(cuFuncSetAttribute(sf, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100));
+      DRV(cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100));
+      unsigned nwords = (unsigned)(max_smem / 4);
+      void* sargs[] = {&nwords};
+      for (int q = 0; q < nq; ++q) {
+        DRV(cuLaunchKernel(sf, nsm, 1, 1, 1024, 1, 1, (unsigned)max_smem, nullptr, sargs, nullptr));
+        CUdeviceptr dq = d_q.p + (CUdeviceptr)q * dim * 4, dr = d_res.p + (CUdeviceptr)q * topk * 4,
+                    dh = d_hits.p + (CUdeviceptr)q * 4;
+        void* qargs[] = {&d_data.p, &dq,         &dr,           &d_graph.p, &d_cand,
+                         &np,       &offset_shift, &n_candidates, &topk,      &search_width,
+                         &d_entries.p, &dh,      &max_iter,     &algo};
+        DRV(cuLaunchKernel(fn, 1, 1, 1, 64, 1, 1, smem, nullptr, qargs, nullptr));
+      }
+      DRV(cuCtxSynchronize());
+      cuModuleUnload(smod);
+    }
     DRV(cuMemcpyDtoH(out, d_res.p, (size_t)nq * topk * 4));
     cuModuleUnload(mod);
   }

@@ -20,6 +20,11 @@
 //       s = fmaf(tc, tc, s) over chunks c (t = p - q, dims l + 32c), then the
 //       shuffle-down tree 16,8,4,2,1 (the reference is built with fmad on).
 //   H5  check_zero is per lane (graph_search.cuh:967,1022-1026,1504-1509).
+//   H7  the visited filter starts empty for every query.  The reference never
+//       clears its `__shared__ uint data[SIZE]` (graph_search.cuh:88), so a
+//       block starts with the bits the previous block on that SM left behind;
+//       run one query per launch on zeroed shared memory, the reference
+//       returns exactly what this restatement returns.
 //   H6  a selected pool slot whose |id| >= np (only possible in the first
 //       iteration when search_width exceeds the valid entries, because the
 //       first selection mask is all ones, graph_search.cuh:969) expands no
@@ -161,7 +166,7 @@ struct SearchArgs {
 };
 
 // One query, one "block" of the reference.
-void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, int32_t* out_ids,
+void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, int32_t hit2, int32_t* out_ids,
                 float* out_dists, orc_counters* cnt) {
   const int L = A.L, R = A.degree, W = A.W;
   const int B = W * R;
@@ -187,7 +192,13 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
         if (A.entry_mode == 0) {
           id = (int)lcg_next(seed[i % 64], (uint32_t)np);
         } else {
-          id = (j < A.leaf_cap) ? A.leaf_pids[(int64_t)hit * A.leaf_cap + j] : np;  // entry.cu:60-69
+          // entry.cu:60-69; entry mode 2 appends the second leaf (hit2) after the first
+          if (j < A.leaf_cap)
+            id = A.leaf_pids[(int64_t)hit * A.leaf_cap + j];
+          else if (A.entry_mode == 2 && hit2 >= 0 && hit2 != hit && j < 2 * A.leaf_cap)
+            id = A.leaf_pids[(int64_t)hit2 * A.leaf_cap + (j - A.leaf_cap)];
+          else
+            id = np;
         }
         batch[i].id = id;
         bloom.add((uint32_t)id);  // :490 adds every entry, padding included
@@ -335,14 +346,15 @@ extern "C" int orc_search(const float* base, int64_t np, int d, const float* que
                           int bloom_words, int bloom_hashes, int entry_mode, int32_t* out_ids,
                           float* out_dists, orc_counters* counters, int n_threads) {
   return orc_search_rerank(base, nullptr, np, d, queries, nq, graph, degree, leaf_pids, leaf_cap,
-                           hits, L, k, search_width, max_iter, bloom_words, bloom_hashes,
+                           hits, nullptr, L, k, search_width, max_iter, bloom_words, bloom_hashes,
                            entry_mode, out_ids, out_dists, counters, n_threads);
 }
 
 extern "C" int orc_search_rerank(const float* base, const float* rerank_base, int64_t np, int d,
                                  const float* queries, int64_t nq, const int32_t* graph,
                                  int degree, const int32_t* leaf_pids, int leaf_cap,
-                                 const int32_t* hits, int L, int k, int search_width, int max_iter,
+                                 const int32_t* hits, const int32_t* hits2, int L, int k,
+                                 int search_width, int max_iter,
                                  int bloom_words, int bloom_hashes, int entry_mode,
                                  int32_t* out_ids, float* out_dists, orc_counters* counters,
                                  int n_threads) {
@@ -351,8 +363,9 @@ extern "C" int orc_search_rerank(const float* base, const float* rerank_base, in
       k > L || search_width <= 0 || max_iter < 0 || bloom_words <= 0 ||
       (bloom_words & (bloom_words - 1)) || bloom_hashes <= 0 || bloom_hashes > 10)
     return -1;
-  if (entry_mode == 1 && (!leaf_pids || !hits || leaf_cap <= 0)) return -1;
-  if (entry_mode != 0 && entry_mode != 1) return -1;
+  if (entry_mode != 0 && (!leaf_pids || !hits || leaf_cap <= 0)) return -1;
+  if (entry_mode == 2 && !hits2) return -1;
+  if (entry_mode < 0 || entry_mode > 2) return -1;
   SearchArgs A{base, rerank_base, np, d, graph, degree, leaf_pids, leaf_cap, L, k, search_width,
                max_iter, bloom_words, bloom_hashes, entry_mode};
 #ifdef _OPENMP
@@ -360,7 +373,8 @@ extern "C" int orc_search_rerank(const float* base, const float* rerank_base, in
 #pragma omp parallel for schedule(dynamic, 4) num_threads(n_threads)
 #endif
   for (int64_t qi = 0; qi < nq; ++qi) {
-    search_one(A, queries + qi * d, qi, entry_mode == 1 ? hits[qi] : 0, out_ids + qi * k,
+    search_one(A, queries + qi * d, qi, entry_mode != 0 ? hits[qi] : 0,
+               entry_mode == 2 ? hits2[qi] : -1, out_ids + qi * k,
                out_dists ? out_dists + qi * k : nullptr, counters ? counters + qi : nullptr);
   }
   (void)n_threads;

@@ -29,7 +29,8 @@ EXPORTS = (
     "rte_build_kdtree", "rte_project", "rte_locate", "rte_search", "rte_search_projected",
     "rte_search_counters", "rte_index_get_info", "rte_get_pca", "rte_get_search_base",
     "rte_get_kdtree", "rte_index_save", "rte_index_load_dir", "rte_index_free", "rte_last_error",
-    "rte_kdtree_build_host", "rte_sym_eig_host", "rte_get_search_base_lowp",
+    "rte_kdtree_build_host", "rte_sym_eig_host", "rte_get_search_base_lowp", "rte_gemm_bf16",
+    "rte_default_train_params", "rte_learned_train", "rte_learned_predict", "rte_mlp_grad_check",
 )
 
 
@@ -48,6 +49,20 @@ class IndexInfo(ctypes.Structure):
                 ("expand_ratio", ctypes.c_float), ("has_bf16", ctypes.c_int),
                 ("has_fp8", ctypes.c_int), ("device", ctypes.c_int),
                 ("device_bytes", ctypes.c_int64)]
+
+
+class TrainParams(ctypes.Structure):
+    _fields_ = [("hidden", ctypes.c_int), ("epochs", ctypes.c_int), ("batch", ctypes.c_int),
+                ("lr", ctypes.c_float), ("label_beam", ctypes.c_int), ("seed", ctypes.c_int)]
+
+
+class TrainReport(ctypes.Structure):
+    _fields_ = [("first_loss", ctypes.c_float), ("last_loss", ctypes.c_float),
+                ("train_acc", ctypes.c_float), ("n_train", ctypes.c_int64),
+                ("classes", ctypes.c_int), ("steps", ctypes.c_int64), ("train_ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class RteError(RuntimeError):
@@ -95,6 +110,11 @@ def load_library(path: str = LIB_PATH):
                                    ctypes.POINTER(i64)], i32),
         "rte_sym_eig_host": ([P, i32, P, P], i32),
         "rte_get_search_base_lowp": ([P, i32, P], i32),
+        "rte_gemm_bf16": ([P, P, i32, i32, i32, P, P], i32),
+        "rte_default_train_params": ([ctypes.POINTER(TrainParams)], None),
+        "rte_learned_train": ([P, P, i64, ctypes.POINTER(TrainParams), ctypes.POINTER(TrainReport)], i32),
+        "rte_learned_predict": ([P, P, i64, P, P], i32),
+        "rte_mlp_grad_check": ([P, P, i32, i32, i32, i32] + [P] * 13, i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -184,6 +204,41 @@ def sym_eig_host(a):
                                            w.ctypes.data_as(ctypes.c_void_p),
                                            v.ctypes.data_as(ctypes.c_void_p)))
     return w, v
+
+
+def bf16_bits(x):
+    """FP32 -> BF16 bit patterns (round to nearest even), as uint16."""
+    b = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    return ((b + 0x7FFF + ((b >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def gemm_bf16(a_bits, b_bits):
+    """C = A @ B.T on the tensor cores; A [M,K], B [N,K] BF16 bit patterns."""
+    a = np.ascontiguousarray(a_bits, np.uint16)
+    b = np.ascontiguousarray(b_bits, np.uint16)
+    M, K = a.shape
+    N = b.shape[0]
+    c = np.empty((M, N), np.float32)
+    _check(load_library().rte_gemm_bf16(a.ctypes.data_as(ctypes.c_void_p),
+                                        b.ctypes.data_as(ctypes.c_void_p), M, N, K,
+                                        c.ctypes.data_as(ctypes.c_void_p), None))
+    return c
+
+
+def mlp_grad_check(X, labels, W1, b1, W2, b2, W3, b3):
+    """GPU forward+backward of the learned-entry MLP -> (grads dict, loss[M])."""
+    X = np.ascontiguousarray(X, np.float32)
+    labels = np.ascontiguousarray(labels, np.int32)
+    ws = [np.ascontiguousarray(w, np.float32) for w in (W1, b1, W2, b2, W3, b3)]
+    M, d = X.shape
+    H, C = ws[0].shape[0], ws[4].shape[0]
+    gs = [np.empty_like(w) for w in ws]
+    loss = np.empty(M, np.float32)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    _check(load_library().rte_mlp_grad_check(p(X), p(labels), M, d, H, C, *[p(w) for w in ws],
+                                             p(gs[0]), p(gs[1]), p(gs[2]), p(gs[3]), p(gs[4]),
+                                             p(gs[5]), p(loss)))
+    return dict(zip(("W1", "b1", "W2", "b2", "W3", "b3"), gs)), loss
 
 
 class Index:
@@ -371,6 +426,30 @@ class Index:
                                              e.ctypes.data_as(ctypes.c_void_p),
                                              p.ctypes.data_as(ctypes.c_void_p)))
         return t, e, p
+
+    def train_learned(self, train_queries, **kw) -> dict:
+        """Train the learned-entry MLP on raw training queries; returns the report."""
+        p = TrainParams()
+        load_library().rte_default_train_params(ctypes.byref(p))
+        for k, v in kw.items():
+            if not hasattr(p, k):
+                raise TypeError(f"unknown training parameter {k}")
+            setattr(p, k, v)
+        tq = _as(train_queries, np.float32, "float32")
+        pq, kq = _ptr(tq)
+        rep = TrainReport()
+        _check(load_library().rte_learned_train(self._h, pq, tq.shape[0], ctypes.byref(p),
+                                                ctypes.byref(rep)))
+        return rep.as_dict()
+
+    def learned_leaves(self, projected, stream=None):
+        projected = _as(projected, np.float32, "float32")
+        out = _empty_like_kind(projected, (projected.shape[0],), np.int32, "int32")
+        pp, kp = _ptr(projected)
+        po, ko = _ptr(out)
+        _check(load_library().rte_learned_predict(self._h, pp, projected.shape[0], po,
+                                                  _stream_ptr(stream)))
+        return out
 
     def save(self, path: str):
         _check(load_library().rte_index_save(self._h, path.encode()))

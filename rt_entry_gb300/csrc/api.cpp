@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "host_build.h"
+#include "index_impl.h"
 #include "index_kernels.h"
 #include "io.h"
 #include "search_dispatch.h"
@@ -24,77 +25,16 @@
 using namespace rte;
 
 namespace {
-
 thread_local std::string g_err;
+int chunks_of(int d) { return (d + 31) / 32; }
+}  // namespace
 
+namespace rte {
 rte_status fail(rte_status s, const std::string& msg) {
   g_err = msg;
   return s;
 }
-
-#define RTE_CUDA(call)                                                                     \
-  do {                                                                                     \
-    cudaError_t e_ = (call);                                                               \
-    if (e_ != cudaSuccess)                                                                 \
-      return fail(e_ == cudaErrorMemoryAllocation ? RTE_ENOMEM : RTE_ECUDA,                \
-                  std::string(#call) + ": " + cudaGetErrorString(e_));                     \
-  } while (0)
-
-template <typename T>
-struct DevBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  DevBuf() = default;
-  DevBuf(const DevBuf&) = delete;
-  DevBuf& operator=(const DevBuf&) = delete;
-  ~DevBuf() { reset(); }
-  void reset() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  cudaError_t alloc(size_t count) {
-    reset();
-    if (count == 0) return cudaSuccess;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-    if (e == cudaSuccess) n = count;
-    return e;
-  }
-  size_t bytes() const { return n * sizeof(T); }
-};
-
-// Device scratch from the stream-ordered pool, released on scope exit
-// (stream-ordered, so the memory is reused only after prior work finishes).
-struct AsyncBuf {
-  void* p = nullptr;
-  cudaStream_t st = nullptr;
-  AsyncBuf() = default;
-  AsyncBuf(const AsyncBuf&) = delete;
-  ~AsyncBuf() {
-    if (p) cudaFreeAsync(p, st);
-  }
-  cudaError_t alloc(size_t bytes, cudaStream_t s) {
-    st = s;
-    if (bytes == 0) bytes = 16;
-    return cudaMallocAsync(&p, bytes, s);
-  }
-  template <typename T>
-  T* as() const {
-    return static_cast<T*>(p);
-  }
-};
-
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    cudaGetDevice(&prev);
-    if (prev != dev) cudaSetDevice(dev);
-  }
-  ~DeviceGuard() {
-    if (prev >= 0) cudaSetDevice(prev);
-  }
-};
-
+void clear_error() { g_err.clear(); }
 // Host or device memory?  Unregistered host memory reports
 // cudaMemoryTypeUnregistered; pinned host memory cudaMemoryTypeHost.
 bool is_device_ptr(const void* p) {
@@ -105,39 +45,9 @@ bool is_device_ptr(const void* p) {
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
-
-int chunks_of(int d) { return (d + 31) / 32; }
-
-}  // namespace
-
-struct rte_index {
-  int device = 0;
-  int num_sms = 0;
-  int64_t np = 0;
-  int dim = 0;
-  int degree = 0;
-  DevBuf<float> raw;      // [np][dim] row-major input vectors
-  DevBuf<int32_t> graph;  // [np][degree]
-  // PCA
-  bool has_pca = false;
-  int search_dim = 0;
-  std::vector<double> mean64, eig64, vec64;  // vec64[dim][dim], column = component
-  std::vector<float> mean32, rot32;          // rot32[dim][dim]
-  DevBuf<float> d_mean, d_rot;               // d_rot[dim][search_dim]
-  // search space
-  int C = 0;
-  DevBuf<float> il32;
-  DevBuf<uint16_t> il16;
-  DevBuf<uint8_t> il8;
-  DevBuf<float> scale8;
-  std::vector<float> xyz;  // first three search-space coordinates [np][3]
-  // kd-tree
-  bool has_kdtree = false;
-  KdTree kd;
-  float expand_ratio = 0.f;
-  DevBuf<BvhNode> d_nodes;
-  DevBuf<int32_t> d_pids;
-};
+rte_status learned_leaves(const rte_index* x, const float* d_proj, int64_t nq, int32_t* d_leaf,
+                          cudaStream_t st);
+}  // namespace rte
 
 namespace {
 
@@ -261,20 +171,30 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
     return fail(RTE_EINVAL, "bloom_words must be a power of two in [32, 16384]");
   if (prm->bloom_hashes < 1 || prm->bloom_hashes > 10) return fail(RTE_EINVAL, "bloom_hashes must be in [1, 10]");
   if (prm->precision < 0 || prm->precision > 2) return fail(RTE_EINVAL, "precision must be 0, 1 or 2");
-  if (prm->entry_mode != RTE_ENTRY_RANDOM && prm->entry_mode != RTE_ENTRY_KDTREE)
-    return fail(RTE_EINVAL, "entry_mode must be RTE_ENTRY_RANDOM or RTE_ENTRY_KDTREE here");
-  if (prm->entry_mode == RTE_ENTRY_KDTREE && !x->has_kdtree)
+  if (prm->entry_mode < RTE_ENTRY_RANDOM || prm->entry_mode > RTE_ENTRY_LEARNED)
+    return fail(RTE_EINVAL, "entry_mode must be RTE_ENTRY_RANDOM, _KDTREE or _LEARNED");
+  if (prm->entry_mode == RTE_ENTRY_LEARNED && !x->mlp.trained)
+    return fail(RTE_ESTATE, "learned entries requested before rte_learned_train");
+  if (prm->entry_mode != RTE_ENTRY_RANDOM && !x->has_kdtree)
     return fail(RTE_ESTATE, "kd-tree entries requested before rte_build_kdtree");
   if (!search_chunks_supported(x->C))
     return fail(RTE_EINVAL, "search dimension " + std::to_string(x->search_dim) + " has no kernel instantiation");
   pl.NL = pl.L / 32;
   pl.NB = B / 32;
   pl.prec = prm->precision;
-  pl.wpb = prm->warps_per_block > 0 ? prm->warps_per_block : 8;
-  if (pl.wpb > 8) return fail(RTE_EINVAL, "warps_per_block must be <= 8");
+  // per warp: the bloom filter plus the compaction buffers (ids, distances)
   const int S = std::max(B, pl.L);
-  pl.smem = (size_t)pl.wpb * (prm->bloom_words + 2 * S) * 4;
-  if (pl.smem > 227 * 1024) return fail(RTE_EINVAL, "bloom filter too large for the block's shared memory");
+  const size_t per_warp = (size_t)(prm->bloom_words + 2 * S) * 4;
+  const size_t smem_cap = 227 * 1024;
+  if (prm->warps_per_block > 0) {
+    pl.wpb = prm->warps_per_block;
+    if (pl.wpb > 8) return fail(RTE_EINVAL, "warps_per_block must be <= 8");
+  } else {
+    pl.wpb = (int)std::min<size_t>(8, smem_cap / per_warp);
+  }
+  pl.smem = (size_t)pl.wpb * per_warp;
+  if (pl.wpb < 1 || pl.smem > smem_cap)
+    return fail(RTE_EINVAL, "bloom filter too large for the block's shared memory");
   const int occ = occupancy_search(x->C, pl.NL, pl.NB, pl.prec, pl.wpb, pl.smem);
   if (occ <= 0)
     return fail(RTE_EINVAL, "no kernel instantiation for beam " + std::to_string(pl.L) + ", batch " +
@@ -301,10 +221,24 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
     qp = proj.as<float>();
   }
   const int32_t* hits = d_hits_in;
+  const int32_t* hits2 = nullptr;
+  AsyncBuf hits2b;
   if (prm->entry_mode == RTE_ENTRY_KDTREE && !hits) {
     RTE_CUDA(hitsb.alloc((size_t)nq * 4, st));
     RTE_CUDA(launch_locate(x->d_nodes.p, qp, nq, x->search_dim, hitsb.as<int32_t>(), st));
     hits = hitsb.as<int32_t>();
+  }
+  if (prm->entry_mode == RTE_ENTRY_LEARNED) {
+    // proposed leaf (MLP) first, kd-tree leaf second
+    RTE_CUDA(hits2b.alloc((size_t)nq * 4, st));
+    RTE_CUDA(launch_locate(x->d_nodes.p, qp, nq, x->search_dim, hits2b.as<int32_t>(), st));
+    hits2 = hits2b.as<int32_t>();
+    if (!hits) {
+      RTE_CUDA(hitsb.alloc((size_t)nq * 4, st));
+      rte_status ls = learned_leaves(x, qp, nq, hitsb.as<int32_t>(), st);
+      if (ls != RTE_OK) return ls;
+      hits = hitsb.as<int32_t>();
+    }
   }
   RTE_CUDA(work.alloc(4, st));
   RTE_CUDA(cudaMemsetAsync(work.p, 0, 4, st));
@@ -317,6 +251,7 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   a.graph = x->graph.p;
   a.leaf_pids = x->has_kdtree ? x->d_pids.p : nullptr;
   a.hits = hits;
+  a.hits2 = hits2;
   a.out_ids = d_ids;
   a.out_dists = d_dists;
   a.counters = d_counters;
@@ -340,6 +275,18 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
 }
 
 }  // namespace
+
+namespace rte {
+rte_status plain_top1(rte_index* x, const float* d_proj, int64_t n, int beam, int32_t* d_ids,
+                      cudaStream_t st) {
+  rte_search_params p;
+  rte_default_params(&p);
+  p.beam = beam;
+  p.k = 1;
+  p.entry_mode = RTE_ENTRY_KDTREE;
+  return run_query_path(x, d_proj, true, nullptr, n, &p, d_ids, nullptr, nullptr, st);
+}
+}  // namespace rte
 
 extern "C" {
 

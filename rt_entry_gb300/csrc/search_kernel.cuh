@@ -356,9 +356,13 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
   __syncwarp();
 
   // ---- entry phase (graph_search.cuh:479-959) ----
-  int hit = a.entry_mode == 1 ? __ldg(a.hits + q) : 0;
+  int hit = a.entry_mode != 0 ? __ldg(a.hits + q) : 0;
   if (hit < 0 || hit >= a.n_leaves) hit = 0;
   const int32_t* lp = a.leaf_pids + (size_t)hit * a.leaf_cap;
+  // learned entries: the proposed leaf's points, then the kd-tree leaf's
+  int hit2 = a.entry_mode == 2 ? __ldg(a.hits2 + q) : -1;
+  if (hit2 >= a.n_leaves || hit2 == hit) hit2 = -1;
+  const int32_t* lp2 = a.leaf_pids + (size_t)(hit2 < 0 ? 0 : hit2) * a.leaf_cap;
   uint32_t seed0 = (uint32_t)q * 64u + (uint32_t)lane;  // reference thread `lane`
   uint32_t seed1 = seed0 + 32u;                           // reference thread `lane + 32`
   constexpr int kEntryBatches = (L + B - 1) / B;
@@ -373,8 +377,10 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
           uint32_t& s = (j & 1) ? seed1 : seed0;
           s = s * 1103515245u + 12345u;
           id = (int)(s % (uint32_t)np);
-        } else {
-          id = pos < a.leaf_cap ? __ldg(lp + pos) : np;
+        } else if (pos < a.leaf_cap) {
+          id = __ldg(lp + pos);
+        } else if (hit2 >= 0 && pos < 2 * a.leaf_cap) {
+          id = __ldg(lp2 + pos - a.leaf_cap);
         }
         bloom.add((uint32_t)id);  // every entry, padding included (:490)
       }

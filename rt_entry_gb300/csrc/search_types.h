@@ -15,6 +15,7 @@ struct SearchArgs {
   const int32_t* graph;     // [np][R], padding np
   const int32_t* leaf_pids; // [n_leaves][leaf_cap], padding np
   const int32_t* hits;      // [nq] leaf per query
+  const int32_t* hits2;     // [nq] second leaf (entry mode 2: the kd-tree leaf)
   int32_t* out_ids;         // [nq][k]
   float* out_dists;         // [nq][k] or null
   long long* counters;      // [nq][4] or null

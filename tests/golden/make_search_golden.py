@@ -10,7 +10,9 @@ Three steps:
       compiled from the reference's graph_search.cuh by oracle/ref/Makefile)
       runs the reference GraphSearchKernel through oracle/ref_launch.cpp and
       writes <outdir>/search_<case>_ref.npy (the returned ids, topk = beam so
-      the whole final pool is pinned).
+      the whole final pool is pinned), and for the kd-tree cases
+      <outdir>/search_<case>_ref_scrub.npy from one launch per query on
+      zeroed shared memory (the reference never clears its bloom filter).
   python tests/golden/make_search_golden.py merge <outdir>
       stores those ids as `ref_ids` inside each fixture.
 """
@@ -87,14 +89,17 @@ def entries_table(leaf_pids, L, np_):
     return t
 
 
-def run_reference(outdir):
+def run_reference(outdir, scrub=False):
+    """scrub: per-query launches on scrubbed shared memory (kd-tree cases),
+    so the reference's uninitialised bloom filter starts empty."""
     import oracle
     lib_path = oracle.build_ref_launcher()
     lib = ctypes.CDLL(lib_path)
     lib.ref_last_error.restype = ctypes.c_char_p
     P = ctypes.c_void_p
     I = ctypes.c_int
-    lib.ref_graph_search.argtypes = [ctypes.c_char_p, P, I, I, P, I, P, I, P, I, I, P, I, I, I, I, P]
+    lib.ref_graph_search.argtypes = [ctypes.c_char_p, P, I, I, P, I, P, I, P, I, I, P, I, I, I, I, I,
+                                     P]
     lib.ref_graph_search.restype = I
     os.makedirs(outdir, exist_ok=True)
     for name, d, *_ in CASES:
@@ -103,15 +108,17 @@ def run_reference(outdir):
         L = int(c["beam"])
         ent = entries_table(c["leaf_pids"], L, base.shape[0])
         hits = c["hits"].astype(np.int32)
+        if scrub and int(c["algo"]) != 1:
+            continue
         out = np.empty((q.shape[0], L), np.int32)
         cubin = os.path.join(oracle.REF_OUT, f"graph_search_d{d}.cubin")
         rc = lib.ref_graph_search(cubin.encode(), base.ctypes.data, base.shape[0], d, q.ctypes.data,
                                   q.shape[0], graph.ctypes.data, graph.shape[1], ent.ctypes.data,
                                   ent.shape[0], L, hits.ctypes.data, L, 1, int(c["max_iter"]),
-                                  int(c["algo"]), out.ctypes.data)
+                                  int(c["algo"]), int(scrub), out.ctypes.data)
         if rc != 0:
             raise RuntimeError(f"{name}: {lib.ref_last_error().decode()}")
-        np.save(os.path.join(outdir, f"search_{name}_ref.npy"), out)
+        np.save(os.path.join(outdir, f"search_{name}_ref{'_scrub' if scrub else ''}.npy"), out)
         print("reference ran", name)
 
 
@@ -120,6 +127,9 @@ def merge(outdir):
         ref = np.load(os.path.join(outdir, f"search_{name}_ref.npy"))
         z = dict(np.load(path_of(name)))
         z["ref_ids"] = ref.astype(np.int32)
+        sp = os.path.join(outdir, f"search_{name}_ref_scrub.npy")
+        if os.path.exists(sp):
+            z["ref_ids_scrub"] = np.load(sp).astype(np.int32)
         np.savez_compressed(path_of(name), **z)
         print("merged", name)
 
@@ -130,6 +140,7 @@ if __name__ == "__main__":
         make_inputs()
     elif cmd == "reference":
         run_reference(sys.argv[2])
+        run_reference(sys.argv[2], scrub=True)
     elif cmd == "merge":
         merge(sys.argv[2])
     else:

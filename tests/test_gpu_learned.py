@@ -1,0 +1,90 @@
+"""Learned entry on the GPU: tensor-core GEMM, MLP gradients against the CPU
+oracle (oracle/mlp_ref.py), training, and the learned-entry search against
+the search oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_tensor_core_gemm_matches_fp64(lib, cuda):
+    import rt_entry_gb300 as r
+    rng = np.random.default_rng(0)
+    for M, N, K in [(128, 128, 64), (100, 70, 96), (513, 257, 264), (256, 4096, 256)]:
+        a = rng.standard_normal((M, K)).astype(np.float32)
+        b = rng.standard_normal((N, K)).astype(np.float32)
+        ab, bb = r.bf16_bits(a), r.bf16_bits(b)
+        af = (ab.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+        bf = (bb.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+        ref = af @ bf.T
+        c = r.gemm_bf16(ab, bb)
+        # exact BF16 products, FP32 accumulation: error ~ K * 2^-24 of the terms
+        assert np.abs(c - ref).max() <= 1e-5 * np.abs(ref).max(), (M, N, K)
+
+
+def test_mlp_gradients_match_oracle(lib, cuda):
+    import rt_entry_gb300 as r
+    from oracle import mlp_ref
+    rng = np.random.default_rng(1)
+    M, d, H, C = 256, 100, 64, 300
+    X = rng.standard_normal((M, d)).astype(np.float32)
+    y = rng.integers(0, C, M).astype(np.int32)
+    W1 = (rng.standard_normal((H, d)) / np.sqrt(d)).astype(np.float32)
+    b1 = (rng.standard_normal(H) * 0.1).astype(np.float32)
+    W2 = (rng.standard_normal((H, H)) / np.sqrt(H)).astype(np.float32)
+    b2 = (rng.standard_normal(H) * 0.1).astype(np.float32)
+    W3 = (rng.standard_normal((C, H)) / np.sqrt(H)).astype(np.float32)
+    b3 = (rng.standard_normal(C) * 0.1).astype(np.float32)
+    g, loss = r.mlp_grad_check(X, y, W1, b1, W2, b2, W3, b3)
+    lref, gref = mlp_ref.loss_and_grads(X, y, W1, b1, W2, b2, W3, b3, bf=True)
+    assert np.allclose(loss, lref, rtol=2e-3, atol=2e-3)
+    # BF16 roundings of intermediates may flip by one BF16 ulp where FP32 and
+    # FP64 accumulation differ; the tolerance is a relative Frobenius norm
+    for name in ("W1", "b1", "W2", "b2", "W3", "b3"):
+        err = np.linalg.norm(g[name] - gref[name]) / max(np.linalg.norm(gref[name]), 1e-30)
+        assert err < 1e-2, (name, err)
+
+
+def _lowrank_clusters(n, nq, d, seed, k=24, rank=6, spread=30.0, noise=3.0, lo=40, hi=215):
+    """Clusters near rank-`rank` subspaces: their PCA-3 footprints overlap, so
+    a kd-tree leaf can belong to the wrong cluster."""
+    crng = np.random.Generator(np.random.Philox(seed))
+    cent = crng.uniform(lo, hi, (k, d))
+    Q = np.stack([np.linalg.qr(crng.standard_normal((d, rank)))[0] for _ in range(k)])
+    rng = np.random.Generator(np.random.Philox(seed + 1))
+    lab = rng.integers(0, k, n + nq)
+    z = rng.standard_normal((n + nq, rank)) * spread
+    x = cent[lab] + np.einsum("mdr,mr->md", Q[lab], z) + noise * rng.standard_normal((n + nq, d))
+    x = np.rint(np.clip(x, 0, 255)).astype(np.float32)
+    return x[:n], x[n:]
+
+
+def test_learned_entry_trains_and_searches(lib, orc, cuda):
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base, q = _lowrank_clusters(20000, 800, 64, seed=11)
+    train, _ = _lowrank_clusters(16384, 1, 64, seed=12)
+    graph = ds.knn_graph(base, 32)
+    gt = ds.ground_truth(base, q, 10)
+    idx = r.Index.from_arrays(base, graph).build_pca().build_kdtree(32, 0.2)
+    rep = idx.train_learned(train, hidden=128, epochs=12, batch=4096, lr=3e-3, label_beam=64)
+    assert rep["classes"] == idx.info.n_leaves
+    assert rep["last_loss"] < 0.6 * rep["first_loss"], rep
+    qp = idx.project(q)
+    learned = idx.learned_leaves(qp)
+    kd = idx.locate(qp)
+    assert learned.shape == kd.shape and ((learned >= 0) & (learned < idx.info.n_leaves)).all()
+    # the learned search is bit-exact with the oracle given the same two leaves
+    pb = idx.search_base()
+    _, _, pids = idx.kdtree()
+    ids, dd = idx.search_projected(qp, beam=64, k=64, entry_mode=r.ENTRY_LEARNED)
+    oids, od = orc.search(pb, qp, graph, L=64, k=64, entry_mode=2, leaf_pids=pids, hits=learned,
+                          hits2=kd)
+    assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
+    assert np.array_equal(dd, od)
+    # what the model gains: recall at a small beam with vs without it
+    rk, _ = idx.search(q, beam=32, k=10)
+    rl, _ = idx.search(q, beam=32, k=10, entry_mode=r.ENTRY_LEARNED)
+    rec_kd = ds.recall_at(rk, gt, 10)
+    rec_l = ds.recall_at(rl, gt, 10)
+    assert rec_l >= rec_kd - 0.01, (rec_l, rec_kd)

@@ -25,8 +25,15 @@ def _cases():
 
 @pytest.mark.parametrize("case", [c[0] for c in _cases().CASES])
 def test_search_oracle_matches_reference_kernel(orc, case):
-    """Ids of the whole final pool equal the reference GraphSearchKernel's,
-    run on a GB300 from a cubin compiled from graph_search.cuh."""
+    """The whole final pool equals the reference GraphSearchKernel's, run on a
+    GB300 from a cubin compiled from graph_search.cuh.
+
+    `ref_ids_scrub`: one launch per query on zeroed shared memory, so the
+    reference's bloom filter (graph_search.cuh:88, never cleared) starts
+    empty as the canonical rule says -> must match exactly.  `ref_ids`: the
+    reference's own batched launch, whose filter starts with the bits left by
+    the previous block on the SM; those extra false positives may change a
+    few queries (bounded here at 5%)."""
     g = _cases()
     c = g.load_case(case)
     if "ref_ids" not in c:
@@ -37,8 +44,13 @@ def test_search_oracle_matches_reference_kernel(orc, case):
                             leaf_pids=c["leaf_pids"], hits=c["hits"])
     ref = c["ref_ids"]
     assert ids.shape == ref.shape
-    mism = (ids != ref).any(axis=1)
-    assert not mism.any(), f"{mism.sum()} of {len(mism)} queries differ"
+    if "ref_ids_scrub" in c:
+        mism = (ids != c["ref_ids_scrub"]).any(axis=1)
+        assert not mism.any(), f"{mism.sum()} of {len(mism)} queries differ (scrubbed)"
+        assert (ids != ref).any(axis=1).mean() <= 0.05
+    else:
+        mism = (ids != ref).any(axis=1)
+        assert not mism.any(), f"{mism.sum()} of {len(mism)} queries differ"
 
 
 def test_search_golden_inputs_are_consistent(orc):
