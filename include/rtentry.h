@@ -139,6 +139,40 @@ rte_status rte_search_projected(rte_index* idx, const float* projected, const in
                                 int64_t nq, const rte_search_params* params, int32_t* out_ids,
                                 float* out_dists, void* stream);
 
+/* ---- uneven query streams (spec form 2; no reference counterpart:
+ * the reference launches each stage separately and synchronises the device
+ * after each, graph.cu:254-337) ----
+ * A batcher captures the whole query path (projection, kd-tree location,
+ * persistent search) once into a CUDA graph sized for max_nq queries; the
+ * kernels read the batch size from device memory, so every batch of up to
+ * max_nq queries replays the same graph.  Random or kd-tree entries. */
+typedef struct rte_batcher rte_batcher;
+rte_status rte_batcher_create(rte_index* idx, int64_t max_nq, const rte_search_params* params,
+                              rte_batcher** out);
+/* queries [nq x dim] (host or device) -> out_ids / out_dists [nq x k]. */
+rte_status rte_batcher_search(rte_batcher* b, const float* queries, int64_t nq, int32_t* out_ids,
+                              float* out_dists, void* stream);
+int rte_batcher_k(const rte_batcher* b);
+void rte_batcher_free(rte_batcher* b);
+
+typedef struct {
+  int met_target;  /* 1 if some candidate reached the recall target          */
+  float recall;    /* k@k recall of the chosen parameters on the sample       */
+  float ms;        /* device time of one search of the sample                 */
+  float qps;
+  int evaluated;   /* candidates measured                                     */
+} rte_autotune_report;
+
+/* Picks beam, search width, bloom filter size and warps per block: every
+ * candidate runs on the sample queries [nq x dim]; recall@k is measured
+ * against gt [nq x gt_k] (true neighbour ids, gt_k >= k); the fastest
+ * candidate reaching target_recall wins (else the one with the best
+ * recall).  Other fields of *params (precision, entry mode, max_iter,
+ * hashes) are kept. */
+rte_status rte_autotune(rte_index* idx, const float* queries, int64_t nq, const int32_t* gt,
+                        int gt_k, int k, float target_recall, rte_search_params* params,
+                        rte_autotune_report* report);
+
 /* Per-query work counters of the last rte_search_projected-equivalent run:
  * [nq x 4] int64 = valid entries, expanded nodes, distance evaluations,
  * iterations.  Runs the search once more with counting enabled. */
@@ -185,8 +219,9 @@ rte_status rte_kdtree_build_host(const float* xyz, int64_t n, int leaf_size, flo
 rte_status rte_sym_eig_host(const double* a, int n, double* w, double* v);
 
 /* ---- learned entry (no reference counterpart; spec form 4) ----
- * A 3-layer MLP (search-space query -> hidden -> hidden -> kd-tree leaf)
- * proposes each query's entry leaf.  With RTE_ENTRY_LEARNED the entry list
+ * A 3-layer MLP (search-space query -> hidden -> hidden -> kd-tree subtree)
+ * proposes the region of each query's entry; point location inside that
+ * subtree picks the entry leaf.  With RTE_ENTRY_LEARNED the entry list
  * is the proposed leaf's points followed by the kd-tree leaf's points (the
  * kd-tree stays the fallback), truncated to the beam. */
 typedef struct {
@@ -196,25 +231,29 @@ typedef struct {
   float lr;        /* Adam learning rate, cosine-decayed to lr/10 (2e-3)      */
   int label_beam;  /* beam of the plain search that labels the queries (64)   */
   int seed;        /* initialisation and shuffling seed (3003)                */
+  int max_classes; /* model output width: the kd-tree nodes at the deepest
+                      level with at most this many nodes (4096); the model
+                      picks that subtree, point location inside it picks the
+                      leaf                                                   */
 } rte_train_params;
 
 typedef struct {
   float first_loss, last_loss; /* mean cross-entropy of the first / last batch */
   float train_acc;             /* top-1 leaf accuracy on one training batch    */
   int64_t n_train;
-  int classes;                 /* output width = kd-tree leaves                */
+  int classes;                 /* output width = kd-tree subtrees at one depth */
   int64_t steps;
   float train_ms;              /* device time of the optimisation loop         */
 } rte_train_report;
 
 void rte_default_train_params(rte_train_params* p);
-/* Labels every training query with the leaf holding the best result of the
- * plain kd-tree search (beam label_beam), then trains the MLP on the GPU
- * with BF16 tensor-core GEMMs (FP32 accumulation), softmax cross-entropy
- * and Adam.  Requires the kd-tree; at most 65536 leaves. */
+/* Labels every training query with the subtree holding the best result of
+ * the plain kd-tree search (beam label_beam), then trains the MLP on the
+ * GPU with BF16 tensor-core GEMMs (FP32 accumulation), softmax
+ * cross-entropy and Adam.  Requires the kd-tree. */
 rte_status rte_learned_train(rte_index* idx, const float* train_queries, int64_t n,
                              const rte_train_params* params, rte_train_report* report);
-/* The MLP's leaf for each projected query [nq x search_dim]. */
+/* The learned entry leaf for each projected query [nq x search_dim]. */
 rte_status rte_learned_predict(rte_index* idx, const float* projected, int64_t nq,
                                int32_t* out_leaf, void* stream);
 

@@ -192,11 +192,15 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
         if (A.entry_mode == 0) {
           id = (int)lcg_next(seed[i % 64], (uint32_t)np);
         } else {
-          // entry.cu:60-69; entry mode 2 appends the second leaf (hit2) after the first
-          if (j < A.leaf_cap)
+          // entry.cu:60-69.  Entry mode 2 (no reference counterpart): the first
+          // leaf's points, at most half the beam, then the second leaf's (hit2).
+          const bool two = A.entry_mode == 2 && hit2 >= 0 && hit2 != hit;
+          const int n_first = two ? std::min(A.leaf_cap, L / 2) : A.leaf_cap;
+          const int n_second = two ? std::min(A.leaf_cap, L - n_first) : 0;
+          if (j < n_first)
             id = A.leaf_pids[(int64_t)hit * A.leaf_cap + j];
-          else if (A.entry_mode == 2 && hit2 >= 0 && hit2 != hit && j < 2 * A.leaf_cap)
-            id = A.leaf_pids[(int64_t)hit2 * A.leaf_cap + (j - A.leaf_cap)];
+          else if (j < n_first + n_second)
+            id = A.leaf_pids[(int64_t)hit2 * A.leaf_cap + (j - n_first)];
           else
             id = np;
         }

@@ -31,6 +31,8 @@ EXPORTS = (
     "rte_get_kdtree", "rte_index_save", "rte_index_load_dir", "rte_index_free", "rte_last_error",
     "rte_kdtree_build_host", "rte_sym_eig_host", "rte_get_search_base_lowp", "rte_gemm_bf16",
     "rte_default_train_params", "rte_learned_train", "rte_learned_predict", "rte_mlp_grad_check",
+    "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
+    "rte_batcher_free", "rte_autotune",
 )
 
 
@@ -53,13 +55,22 @@ class IndexInfo(ctypes.Structure):
 
 class TrainParams(ctypes.Structure):
     _fields_ = [("hidden", ctypes.c_int), ("epochs", ctypes.c_int), ("batch", ctypes.c_int),
-                ("lr", ctypes.c_float), ("label_beam", ctypes.c_int), ("seed", ctypes.c_int)]
+                ("lr", ctypes.c_float), ("label_beam", ctypes.c_int), ("seed", ctypes.c_int),
+                ("max_classes", ctypes.c_int)]
 
 
 class TrainReport(ctypes.Structure):
     _fields_ = [("first_loss", ctypes.c_float), ("last_loss", ctypes.c_float),
                 ("train_acc", ctypes.c_float), ("n_train", ctypes.c_int64),
                 ("classes", ctypes.c_int), ("steps", ctypes.c_int64), ("train_ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class AutotuneReport(ctypes.Structure):
+    _fields_ = [("met_target", ctypes.c_int), ("recall", ctypes.c_float), ("ms", ctypes.c_float),
+                ("qps", ctypes.c_float), ("evaluated", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -115,6 +126,12 @@ def load_library(path: str = LIB_PATH):
         "rte_learned_train": ([P, P, i64, ctypes.POINTER(TrainParams), ctypes.POINTER(TrainReport)], i32),
         "rte_learned_predict": ([P, P, i64, P, P], i32),
         "rte_mlp_grad_check": ([P, P, i32, i32, i32, i32] + [P] * 13, i32),
+        "rte_batcher_create": ([P, i64, SP, PP], i32),
+        "rte_batcher_search": ([P, P, i64, P, P, P], i32),
+        "rte_batcher_k": ([P], i32),
+        "rte_batcher_free": ([P], None),
+        "rte_autotune": ([P, P, i64, P, i32, i32, ctypes.c_float, SP,
+                          ctypes.POINTER(AutotuneReport)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -451,5 +468,55 @@ class Index:
                                                   _stream_ptr(stream)))
         return out
 
+    def autotune(self, queries, gt, k: int, target_recall: float = 0.95, **base):
+        """Fastest (beam, width, bloom, warps/block) reaching the recall target."""
+        p = default_params(**base)
+        q = _as(queries, np.float32, "float32")
+        g = np.ascontiguousarray(gt, np.int32)
+        pq, kq = _ptr(q)
+        rep = AutotuneReport()
+        _check(load_library().rte_autotune(self._h, pq, q.shape[0], g.ctypes.data_as(ctypes.c_void_p),
+                                           g.shape[1], k, target_recall, ctypes.byref(p),
+                                           ctypes.byref(rep)))
+        return p, rep.as_dict()
+
+    def batcher(self, max_nq: int, params: SearchParams | None = None, **kw) -> "Batcher":
+        return Batcher(self, max_nq, self._params(params, kw))
+
     def save(self, path: str):
         _check(load_library().rte_index_save(self._h, path.encode()))
+
+
+class Batcher:
+    """CUDA-graph replay of the whole query path for batches of <= max_nq."""
+
+    def __init__(self, index: Index, max_nq: int, params: SearchParams):
+        self.index = index
+        self._h = ctypes.c_void_p()
+        _check(load_library().rte_batcher_create(index._h, max_nq, ctypes.byref(params),
+                                                 ctypes.byref(self._h)))
+        self.k = load_library().rte_batcher_k(self._h)
+
+    def search(self, queries, out_ids=None, out_dists=None, stream=None):
+        q = _as(queries, np.float32, "float32")
+        nq = q.shape[0]
+        if out_ids is None:
+            out_ids = _empty_like_kind(q, (nq, self.k), np.int32, "int32")
+        if out_dists is None:
+            out_dists = _empty_like_kind(q, (nq, self.k), np.float32, "float32")
+        pq, kq = _ptr(q)
+        pi, ki = _ptr(out_ids)
+        pd, kd = _ptr(out_dists)
+        _check(load_library().rte_batcher_search(self._h, pq, nq, pi, pd, _stream_ptr(stream)))
+        return out_ids, out_dists
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().rte_batcher_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

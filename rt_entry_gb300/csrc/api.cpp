@@ -277,6 +277,22 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
 }  // namespace
 
 namespace rte {
+// Launch plan of a search, for entry points defined in other files.
+rte_status search_plan(const rte_index* x, const rte_search_params* prm, int64_t nq, int* L, int* k,
+                       int* NL, int* NB, int* wpb, int* grid, size_t* smem) {
+  Plan pl;
+  rte_status s = plan_search(x, prm, nq, pl);
+  if (s != RTE_OK) return s;
+  *L = pl.L;
+  *k = pl.k;
+  *NL = pl.NL;
+  *NB = pl.NB;
+  *wpb = pl.wpb;
+  *grid = pl.grid;
+  *smem = pl.smem;
+  return RTE_OK;
+}
+
 rte_status plain_top1(rte_index* x, const float* d_proj, int64_t n, int beam, int32_t* d_ids,
                       cudaStream_t st) {
   rte_search_params p;

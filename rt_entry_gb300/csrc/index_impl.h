@@ -101,6 +101,12 @@ struct Mlp {
   float in_scale = 1.f;
   DevBuf<float> W[3], b[3];   // FP32 master weights: W1 [hidden x dp], W2 [hidden x hidden], W3 [classes x hidden]
   DevBuf<uint16_t> W16[3];    // BF16 copies used by the GEMMs
+  // classes are kd-tree nodes at one depth (leaves above it are their own
+  // class): class c covers the subtree of node class_node[c], whose first
+  // leaf in pre-order is class_leaf0[c]
+  int real_classes = 0;
+  int depth = 0;
+  DevBuf<int32_t> class_node, class_leaf0;
 };
 
 }  // namespace rte

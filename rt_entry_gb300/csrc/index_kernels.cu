@@ -115,7 +115,10 @@ constexpr int kPrK = 32;
 
 __global__ void project_rows(const float* __restrict__ x, int64_t n, int d, int xstride,
                              const float* __restrict__ mean, const float* __restrict__ V, int vstride,
-                             int k, float* __restrict__ out, int ostride) {
+                             int k, float* __restrict__ out, int ostride,
+                             const int* __restrict__ n_dev) {
+  if (n_dev) n = min(n, (int64_t)*n_dev);  // graph replay: rows beyond the batch are idle
+  if ((int64_t)blockIdx.x * kPrRows >= n) return;
   __shared__ float sx[kPrRows][kPrK + 1];
   __shared__ float sv[kPrK][kPrCols];
   const int64_t row0 = (int64_t)blockIdx.x * kPrRows;
@@ -234,8 +237,10 @@ __global__ void dequant_rows(const void* __restrict__ il, const float* __restric
 // order, so the first leaf whose box contains the point is the smallest such
 // index (canonical rule for the ray cast's arbitrary hit).
 __global__ void locate_points(const BvhNode* __restrict__ nodes, const float* __restrict__ pts,
-                              int64_t n, int stride, int32_t* __restrict__ out) {
+                              int64_t n, int stride, int32_t* __restrict__ out,
+                              const int* __restrict__ n_dev) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n_dev) n = min(n, (int64_t)*n_dev);
   if (i >= n) return;
   const float x = pts[i * stride + 0], y = pts[i * stride + 1], z = pts[i * stride + 2];
   int stack[kBvhMaxDepth];
@@ -258,7 +263,49 @@ __global__ void locate_points(const BvhNode* __restrict__ nodes, const float* __
   out[i] = hit;
 }
 
+// Point location inside one subtree per point: the traversal starts at
+// start_node[cls[i]] instead of the root; when no leaf box of that subtree
+// contains the point, the subtree's first leaf (fallback_leaf[cls[i]]).
+// Used by the learned entry, whose model predicts the subtree.
+__global__ void locate_in_subtree(const BvhNode* __restrict__ nodes, const float* __restrict__ pts,
+                                  int64_t n, int stride, const int32_t* __restrict__ cls,
+                                  const int32_t* __restrict__ start_node,
+                                  const int32_t* __restrict__ fallback_leaf,
+                                  int32_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = cls[i];
+  const float x = pts[i * stride + 0], y = pts[i * stride + 1], z = pts[i * stride + 2];
+  int stack[kBvhMaxDepth];
+  int sp = 0;
+  stack[sp++] = start_node[c];
+  int32_t hit = fallback_leaf[c];
+  while (sp > 0) {
+    const BvhNode nd = nodes[stack[--sp]];
+    if (!(nd.lo[0] <= x && x <= nd.hi[0] && nd.lo[1] <= y && y <= nd.hi[1] && nd.lo[2] <= z &&
+          z <= nd.hi[2]))
+      continue;
+    if (nd.left < 0) {
+      hit = -nd.left - 1;
+      break;
+    }
+    if (sp + 2 > kBvhMaxDepth) break;
+    stack[sp++] = nd.right;
+    stack[sp++] = nd.left;
+  }
+  out[i] = hit;
+}
+
 // -------------------------------------------------------------- launches ----
+cudaError_t launch_locate_in_subtree(const BvhNode* nodes, const float* pts, int64_t n, int stride,
+                                     const int32_t* cls, const int32_t* start_node,
+                                     const int32_t* fallback_leaf, int32_t* out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  locate_in_subtree<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(nodes, pts, n, stride, cls,
+                                                                  start_node, fallback_leaf, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_mean(const float* x, int64_t n, int d, double* partial, int nblocks,
                         double* mean, cudaStream_t st) {
   const int64_t rpb = (n + nblocks - 1) / nblocks;
@@ -282,7 +329,15 @@ cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const 
                            cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  project_rows<<<grid, 256, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride);
+  project_rows<<<grid, 256, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, int d, int xstride,
+                               const float* mean, const float* V, int vstride, int k, float* out,
+                               int ostride, cudaStream_t st) {
+  dim3 grid((unsigned)((cap + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
+  project_rows<<<grid, 256, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride, n_dev);
   return cudaGetLastError();
 }
 
@@ -313,7 +368,13 @@ cudaError_t launch_dequant(const void* il, const float* scale8, int precision, i
 cudaError_t launch_locate(const BvhNode* nodes, const float* pts, int64_t n, int stride,
                           int32_t* out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  locate_points<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(nodes, pts, n, stride, out);
+  locate_points<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(nodes, pts, n, stride, out, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_locate_dyn(const BvhNode* nodes, const float* pts, int64_t cap, const int* n_dev,
+                              int stride, int32_t* out, cudaStream_t st) {
+  locate_points<<<(unsigned)((cap + 127) / 128), 128, 0, st>>>(nodes, pts, cap, stride, out, n_dev);
   return cudaGetLastError();
 }
 

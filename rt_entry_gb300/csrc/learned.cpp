@@ -96,8 +96,8 @@ cudaError_t gemm(const void* A, const void* B, int M, int N, int K, int epi, voi
 
 int round8(int v) { return (v + 7) & ~7; }
 
-// MLP forward for nq rows of X (BF16 [nq x dp]) -> leaf per row.
-rte_status mlp_predict_bf16(const rte_index* x, const uint16_t* X, int64_t nq, int32_t* d_leaf,
+// MLP forward for nq rows of X (BF16 [nq x dp]) -> class (subtree) per row.
+rte_status mlp_predict_bf16(const rte_index* x, const uint16_t* X, int64_t nq, int32_t* d_cls,
                             int* d_err, cudaStream_t st) {
   const Mlp& m = x->mlp;
   AsyncBuf h1, h2, keys;
@@ -111,8 +111,45 @@ rte_status mlp_predict_bf16(const rte_index* x, const uint16_t* X, int64_t nq, i
                 m.b[1].p, nullptr, d_err, st));
   RTE_CUDA(gemm(h2.p, m.W16[2].p, (int)nq, m.classes, m.hidden, kEpiBiasArgmax, nullptr, 0,
                 m.b[2].p, keys.as<unsigned long long>(), d_err, st));
-  RTE_CUDA(launch_argmax_to_leaf(keys.as<unsigned long long>(), (int)nq, nullptr, d_leaf, st));
+  RTE_CUDA(launch_argmax_to_leaf(keys.as<unsigned long long>(), (int)nq, nullptr, d_cls, st));
   return RTE_OK;
+}
+
+// Classes of the learned head: the kd-tree nodes at `depth` (or leaves above
+// it), numbered in pre-order, left first.
+void subtree_classes(const KdTree& t, int depth, std::vector<int32_t>& leaf_class,
+                     std::vector<int32_t>& class_node, std::vector<int32_t>& class_leaf0) {
+  leaf_class.assign(t.n_leaves, 0);
+  class_node.clear();
+  class_leaf0.clear();
+  std::vector<std::pair<int, int>> st{{0, 0}};  // (node, depth)
+  while (!st.empty()) {
+    auto [nd, dep] = st.back();
+    st.pop_back();
+    const BvhNode& N = t.nodes[nd];
+    if (dep == depth || N.left < 0) {
+      const int32_t c = (int32_t)class_node.size();
+      class_node.push_back(nd);
+      class_leaf0.push_back(-1);
+      std::vector<int> sub{nd};
+      while (!sub.empty()) {  // pre-order, left first: the first leaf met is the smallest
+        const int m = sub.back();
+        sub.pop_back();
+        const BvhNode& Q = t.nodes[m];
+        if (Q.left < 0) {
+          const int32_t leaf = -Q.left - 1;
+          leaf_class[leaf] = c;
+          if (class_leaf0[c] < 0) class_leaf0[c] = leaf;
+        } else {
+          sub.push_back(Q.right);
+          sub.push_back(Q.left);
+        }
+      }
+      continue;
+    }
+    st.push_back({N.right, dep + 1});
+    st.push_back({N.left, dep + 1});
+  }
 }
 
 // Buffers of one optimisation step on a batch of M rows.
@@ -190,7 +227,14 @@ rte_status learned_leaves(const rte_index* x, const float* d_proj, int64_t nq, i
   RTE_CUDA(err.alloc(4, st));
   RTE_CUDA(cudaMemsetAsync(err.p, 0, 4, st));
   RTE_CUDA(launch_cast_rows_bf16(d_proj, nq, m.d_in, x->search_dim, m.in_scale, m.dp, xb.p, st));
-  return mlp_predict_bf16(x, xb.as<uint16_t>(), nq, d_leaf, err.as<int>(), st);
+  AsyncBuf cls;
+  RTE_CUDA(cls.alloc((size_t)nq * 4, st));
+  rte_status s = mlp_predict_bf16(x, xb.as<uint16_t>(), nq, cls.as<int32_t>(), err.as<int>(), st);
+  if (s != RTE_OK) return s;
+  // the model picks the subtree, the kd-tree picks the leaf inside it
+  RTE_CUDA(launch_locate_in_subtree(x->d_nodes.p, d_proj, nq, x->search_dim, cls.as<int32_t>(),
+                                    m.class_node.p, m.class_leaf0.p, d_leaf, st));
+  return RTE_OK;
 }
 
 // Plain-search top-1 for each projected query (device arrays) -> ids.
@@ -207,6 +251,7 @@ extern "C" void rte_default_train_params(rte_train_params* p) {
   p->lr = 2e-3f;
   p->label_beam = 64;
   p->seed = 3003;
+  p->max_classes = 4096;
 }
 
 extern "C" rte_status rte_learned_train(rte_index* x, const float* train_queries, int64_t n,
@@ -218,10 +263,14 @@ extern "C" rte_status rte_learned_train(rte_index* x, const float* train_queries
       !(tp->lr > 0.f) || tp->label_beam <= 0)
     return fail(RTE_EINVAL, "bad training parameters (hidden % 8 == 0, batch % 128 == 0)");
   if (n < tp->batch) return fail(RTE_EINVAL, "fewer training queries than one batch");
-  const int64_t C = x->kd.n_leaves;
-  if (C > 65536)
-    return fail(RTE_EINVAL, "learned head supports at most 65536 leaves; build the kd-tree with a "
-                            "larger leaf_size");
+  if (tp->max_classes < 2 || tp->max_classes > 65536)
+    return fail(RTE_EINVAL, "max_classes must be in [2, 65536]");
+  // classes: kd-tree nodes at the deepest level with at most max_classes nodes
+  int depth = 0;
+  while ((2 << depth) <= tp->max_classes) ++depth;
+  std::vector<int32_t> leaf_class, class_node, class_leaf0;
+  subtree_classes(x->kd, depth, leaf_class, class_node, class_leaf0);
+  const int64_t C = (int64_t)class_node.size();
   DeviceGuard guard(x->device);
   cudaStream_t st = nullptr;
   const int H = tp->hidden, d = x->search_dim, dp = round8(d), M = tp->batch;
@@ -248,7 +297,8 @@ extern "C" rte_status rte_learned_train(rte_index* x, const float* train_queries
       const int32_t p = x->kd.pids[l * x->kd.cap + j];
       if (p < x->np) leaf_of[p] = (int32_t)l;
     }
-  for (int64_t i = 0; i < n; ++i) labels[i] = (ids[i] >= 0 && ids[i] < x->np) ? leaf_of[ids[i]] : 0;
+  for (int64_t i = 0; i < n; ++i)
+    labels[i] = leaf_class[(ids[i] >= 0 && ids[i] < x->np) ? leaf_of[ids[i]] : 0];
   DevBuf<int32_t> d_labels;
   RTE_CUDA(d_labels.alloc(n));
   RTE_CUDA(cudaMemcpy(d_labels.p, labels.data(), n * 4, cudaMemcpyHostToDevice));
@@ -267,10 +317,14 @@ extern "C" rte_status rte_learned_train(rte_index* x, const float* train_queries
   m.d_in = d;
   m.dp = dp;
   m.hidden = H;
-  m.classes = (int)C;
+  // class dimension padded to a multiple of 8 (16-byte TMA row pitch of the
+  // logits / dlogits); padded classes have bias -1e30: zero probability,
+  // zero gradient, never the argmax
+  const int64_t Cp = round8((int)C);
+  m.classes = (int)Cp;
   m.in_scale = in_scale;
-  const int64_t wn[3] = {(int64_t)H * dp, (int64_t)H * H, C * H};
-  const int64_t bn[3] = {H, H, C};
+  const int64_t wn[3] = {(int64_t)H * dp, (int64_t)H * H, Cp * H};
+  const int64_t bn[3] = {H, H, Cp};
   const int fan[3] = {d, H, H};
   DevBuf<float> mw[3], vw[3], mb[3], vb[3], gw[3], gb[3];
   std::mt19937 rng((uint32_t)tp->seed);
@@ -282,11 +336,16 @@ extern "C" rte_status rte_learned_train(rte_index* x, const float* train_queries
     if (l == 0)  // padded input columns stay zero
       for (int r = 0; r < H; ++r)
         for (int c = d; c < dp; ++c) w[(int64_t)r * dp + c] = 0.f;
+    if (l == 2)  // padded classes: zero weights
+      for (int64_t i = C * H; i < Cp * H; ++i) w[i] = 0.f;
+    std::vector<float> bias(bn[l], 0.f);
+    if (l == 2)
+      for (int64_t i = C; i < Cp; ++i) bias[i] = -1e30f;
     RTE_CUDA(m.W[l].alloc(wn[l]));
     RTE_CUDA(m.W16[l].alloc(wn[l]));
     RTE_CUDA(m.b[l].alloc(bn[l]));
     RTE_CUDA(cudaMemcpy(m.W[l].p, w.data(), wn[l] * 4, cudaMemcpyHostToDevice));
-    RTE_CUDA(cudaMemset(m.b[l].p, 0, bn[l] * 4));
+    RTE_CUDA(cudaMemcpy(m.b[l].p, bias.data(), bn[l] * 4, cudaMemcpyHostToDevice));
     RTE_CUDA(launch_f32_to_bf16(m.W[l].p, wn[l], m.W16[l].p, st));
     for (DevBuf<float>* b : {&mw[l], &vw[l], &gw[l]}) {
       RTE_CUDA(b->alloc(wn[l]));
@@ -299,7 +358,7 @@ extern "C" rte_status rte_learned_train(rte_index* x, const float* train_queries
   }
   // 5. per-batch buffers
   StepBufs sb;
-  s = sb.alloc(M, H, (int)C, dp);
+  s = sb.alloc(M, H, (int)Cp, dp);
   if (s != RTE_OK) return s;
   DevBuf<uint16_t> Xb;
   DevBuf<int32_t> yb;
@@ -360,7 +419,13 @@ extern "C" rte_status rte_learned_train(rte_index* x, const float* train_queries
   RTE_CUDA(cudaMemcpy(&herr, err.p, 4, cudaMemcpyDeviceToHost));
   if (herr) return fail(RTE_ETIMEOUT, "a GEMM pipeline wait ran out during training");
   m.trained = true;
-  // training accuracy on the first batch of the last permutation
+  m.real_classes = (int)C;
+  m.depth = depth;
+  RTE_CUDA(m.class_node.alloc(C));
+  RTE_CUDA(m.class_leaf0.alloc(C));
+  RTE_CUDA(cudaMemcpy(m.class_node.p, class_node.data(), C * 4, cudaMemcpyHostToDevice));
+  RTE_CUDA(cudaMemcpy(m.class_leaf0.p, class_leaf0.data(), C * 4, cudaMemcpyHostToDevice));
+  // training accuracy (of the class) on the first batch of the last permutation
   {
     DevBuf<int32_t> pred;
     RTE_CUDA(pred.alloc(M));
@@ -430,15 +495,18 @@ extern "C" rte_status rte_mlp_grad_check(const float* X, const int32_t* labels, 
   m.d_in = d;
   m.dp = round8(d);
   m.hidden = hidden;
-  m.classes = classes;
+  const int Cp = round8(classes);  // padded as in training
+  m.classes = Cp;
   const int H = hidden, dp = m.dp;
-  const int64_t wn[3] = {(int64_t)H * dp, (int64_t)H * H, (int64_t)classes * H};
-  const int64_t bn[3] = {H, H, classes};
-  std::vector<float> w1p(wn[0], 0.f);
+  const int64_t wn[3] = {(int64_t)H * dp, (int64_t)H * H, (int64_t)Cp * H};
+  const int64_t bn[3] = {H, H, Cp};
+  std::vector<float> w1p(wn[0], 0.f), w3p(wn[2], 0.f), b3p(Cp, -1e30f);
   for (int r = 0; r < H; ++r)
     for (int c = 0; c < d; ++c) w1p[(int64_t)r * dp + c] = W1[(int64_t)r * d + c];
-  const float* wsrc[3] = {w1p.data(), W2, W3};
-  const float* bsrc[3] = {b1, b2, b3};
+  std::copy(W3, W3 + (int64_t)classes * H, w3p.begin());
+  std::copy(b3, b3 + classes, b3p.begin());
+  const float* wsrc[3] = {w1p.data(), W2, w3p.data()};
+  const float* bsrc[3] = {b1, b2, b3p.data()};
   DevBuf<float> gw[3], gb[3];
   for (int l = 0; l < 3; ++l) {
     RTE_CUDA(m.W[l].alloc(wn[l]));
@@ -463,7 +531,7 @@ extern "C" rte_status rte_mlp_grad_check(const float* X, const int32_t* labels, 
   RTE_CUDA(cudaMemcpy(y.p, labels, (size_t)M * 4, cudaMemcpyHostToDevice));
   RTE_CUDA(launch_cast_rows_bf16(x32.p, M, d, d, 1.0f, dp, xb.p, st));
   StepBufs sb;
-  rte_status s = sb.alloc(M, H, classes, dp);
+  rte_status s = sb.alloc(M, H, Cp, dp);
   if (s != RTE_OK) return s;
   float* const gwp[3] = {gw[0].p, gw[1].p, gw[2].p};
   float* const gbp[3] = {gb[0].p, gb[1].p, gb[2].p};
@@ -478,10 +546,10 @@ extern "C" rte_status rte_mlp_grad_check(const float* X, const int32_t* labels, 
   for (int r = 0; r < H; ++r)
     for (int c = 0; c < d; ++c) gW1[(int64_t)r * d + c] = g1[(int64_t)r * dp + c];
   RTE_CUDA(cudaMemcpy(gW2, gw[1].p, wn[1] * 4, cudaMemcpyDeviceToHost));
-  RTE_CUDA(cudaMemcpy(gW3, gw[2].p, wn[2] * 4, cudaMemcpyDeviceToHost));
+  RTE_CUDA(cudaMemcpy(gW3, gw[2].p, (size_t)classes * H * 4, cudaMemcpyDeviceToHost));
   RTE_CUDA(cudaMemcpy(gb1, gb[0].p, bn[0] * 4, cudaMemcpyDeviceToHost));
   RTE_CUDA(cudaMemcpy(gb2, gb[1].p, bn[1] * 4, cudaMemcpyDeviceToHost));
-  RTE_CUDA(cudaMemcpy(gb3, gb[2].p, bn[2] * 4, cudaMemcpyDeviceToHost));
+  RTE_CUDA(cudaMemcpy(gb3, gb[2].p, (size_t)classes * 4, cudaMemcpyDeviceToHost));
   if (loss) RTE_CUDA(cudaMemcpy(loss, sb.loss.p, (size_t)M * 4, cudaMemcpyDeviceToHost));
   return RTE_OK;
 }

@@ -236,20 +236,32 @@ __device__ __forceinline__ float lane_partial(const float (&p)[C], const float (
 template <int C, int PREC>
 __device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)[C],
                                           const int* s_ids, float* s_dist, int n, int lane) {
-  constexpr int G = C <= 4 ? 16 : 8;
+  constexpr int G = C <= 4 ? 8 : 2;
   constexpr int SPAN = 32 / G;  // lanes sharing one row after the butterfly
+  // Every valid row is requested into L2 up front (128-byte lines spread
+  // over the lanes), so the groups below find their rows in flight or in L2
+  // instead of paying one memory latency each.
+  {
+    constexpr int kRowBytes = 32 * C * (PREC == kPrecF32 ? 4 : PREC == kPrecBF16 ? 2 : 1);
+    constexpr int kLines = (kRowBytes + 127) / 128;
+    const char* rows = PREC == kPrecF32    ? reinterpret_cast<const char*>(a.base)
+                       : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
+                                           : reinterpret_cast<const char*>(a.base_fp8);
+    for (int i = lane; i < n * kLines; i += 32) {
+      const int row = i / kLines, line = i - row * kLines;
+      const char* p = rows + (size_t)s_ids[row] * kRowBytes + line * 128;
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+    }
+  }
   for (int g0 = 0; g0 < n; g0 += G) {
+    // all G loads first, unconditionally (a short group re-reads its first
+    // row), so they are issued back to back before any use
+    RowLoader<C, PREC> r[G];
+#pragma unroll
+    for (int t = 0; t < G; ++t) r[t].load(a, s_ids[g0 + t < n ? g0 + t : g0], lane);
     float part[G];
 #pragma unroll
-    for (int t = 0; t < G; ++t) {
-      if (g0 + t < n) {
-        RowLoader<C, PREC> r;
-        r.load(a, s_ids[g0 + t], lane);
-        part[t] = lane_partial<C>(r.v, qv);
-      } else {
-        part[t] = 0.0f;
-      }
-    }
+    for (int t = 0; t < G; ++t) part[t] = g0 + t < n ? lane_partial<C>(r[t].v, qv) : 0.0f;
 #pragma unroll
     for (int off = 16, half = G / 2; half >= 1; off >>= 1, half >>= 1) {
       const bool up = (lane & off) != 0;
@@ -363,6 +375,10 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
   int hit2 = a.entry_mode == 2 ? __ldg(a.hits2 + q) : -1;
   if (hit2 >= a.n_leaves || hit2 == hit) hit2 = -1;
   const int32_t* lp2 = a.leaf_pids + (size_t)(hit2 < 0 ? 0 : hit2) * a.leaf_cap;
+  // entry slots: the first leaf's points (at most half the beam when a second
+  // leaf follows), then the second leaf's points
+  const int n_first = hit2 >= 0 ? min(a.leaf_cap, L / 2) : a.leaf_cap;
+  const int n_second = hit2 >= 0 ? min(a.leaf_cap, L - n_first) : 0;
   uint32_t seed0 = (uint32_t)q * 64u + (uint32_t)lane;  // reference thread `lane`
   uint32_t seed1 = seed0 + 32u;                           // reference thread `lane + 32`
   constexpr int kEntryBatches = (L + B - 1) / B;
@@ -377,10 +393,10 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
           uint32_t& s = (j & 1) ? seed1 : seed0;
           s = s * 1103515245u + 12345u;
           id = (int)(s % (uint32_t)np);
-        } else if (pos < a.leaf_cap) {
+        } else if (pos < n_first) {
           id = __ldg(lp + pos);
-        } else if (hit2 >= 0 && pos < 2 * a.leaf_cap) {
-          id = __ldg(lp2 + pos - a.leaf_cap);
+        } else if (hit2 >= 0 && pos < n_first + n_second) {
+          id = __ldg(lp2 + pos - n_first);
         }
         bloom.add((uint32_t)id);  // every entry, padding included (:490)
       }
@@ -532,7 +548,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
 }
 
 template <int C, int NL, int NB, int PREC>
-__global__ void __launch_bounds__(256, 3) search_kernel(SearchArgs a) {
+__global__ void __launch_bounds__(256, (C <= 4 ? 4 : 2)) search_kernel(SearchArgs a) {
   extern __shared__ uint32_t smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -548,11 +564,12 @@ __global__ void __launch_bounds__(256, 3) search_kernel(SearchArgs a) {
   bloom.nh = a.bloom_hashes;
   int* s_ids = reinterpret_cast<int*>(wbase + a.bloom_words);
   float* s_dist = reinterpret_cast<float*>(s_ids + S);
+  const int nq = a.nq_dev ? *a.nq_dev : a.nq;
   for (;;) {
     int q = 0;
     if (lane == 0) q = (int)atomicAdd(a.work, 1u);
     q = __shfl_sync(kFull, q, 0);
-    if (q >= a.nq) break;
+    if (q >= nq) break;
     search_query<C, NL, NB, PREC>(a, q, lane, bloom, s_ids, s_dist);
   }
 }

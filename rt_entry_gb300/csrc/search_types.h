@@ -23,6 +23,7 @@ struct SearchArgs {
   int np, d, qstride, nq, R, W, k, max_iter, bloom_words, bloom_hashes, leaf_cap, entry_mode;
   int rerank;
   int n_leaves;             // hits outside [0, n_leaves) fall back to leaf 0
+  const int* nq_dev;        // if set, the query count is read here (graph replay)
 };
 
 }  // namespace rte

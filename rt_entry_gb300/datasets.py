@@ -56,6 +56,34 @@ class Mixture:
 
 
 @dataclass
+class SubspaceMixture:
+    """Gaussian mixture whose clusters are flat: cluster k is centre_k +
+    bases_k z + noise with z ~ N(0, s^2 I_rank); the centres themselves lie on
+    a low-dimensional subspace, so neighbouring clusters overlap and the kNN
+    graph stays connected (a low intrinsic dimension, as SIFT-like data has)."""
+    centers: np.ndarray   # [K, d]
+    bases: np.ndarray     # [K, d, rank], orthonormal columns
+    s: float
+    noise: float
+    post: str = "round_clip255"
+
+    def sample(self, n: int, seed: int, chunk: int = 1 << 17) -> np.ndarray:
+        rng = _rng(seed)
+        K, d = self.centers.shape
+        rank = self.bases.shape[2]
+        out = np.empty((n, d), np.float32)
+        for s0 in range(0, n, chunk):
+            e = min(n, s0 + chunk)
+            m = e - s0
+            lab = rng.integers(0, K, m)
+            z = rng.standard_normal((m, rank), np.float32) * np.float32(self.s)
+            x = self.centers[lab] + np.einsum("mdr,mr->md", self.bases[lab], z)
+            x += np.float32(self.noise) * rng.standard_normal((m, d), np.float32)
+            out[s0:e] = np.rint(np.clip(x, 0, 255)) if self.post == "round_clip255" else x
+        return out
+
+
+@dataclass
 class Workload:
     name: str
     base: np.ndarray
@@ -76,9 +104,13 @@ def mixture_config(cfg: int, d: int | None = None) -> Mixture:
     if cfg == 1:   # 64 components, centres U[0,100]^d, sigma 5
         d = d or 128
         return Mixture(rng.uniform(0, 100, (64, d)).astype(np.float32), 5.0)
-    if cfg == 2:   # 256 clusters, integer values 0..255 (SIFT-like bvecs)
+    if cfg == 2:   # 256 flat clusters, integer values 0..255 (SIFT-like bvecs)
         d = d or 128
-        return Mixture(rng.uniform(32, 224, (256, d)).astype(np.float32), 64.0, "round_clip255")
+        K, cdim, rank = 256, 8, 16
+        B = np.linalg.qr(rng.standard_normal((d, cdim)))[0]
+        cent = 128.0 + (rng.standard_normal((K, cdim)) * 50.0) @ B.T
+        bases = np.stack([np.linalg.qr(rng.standard_normal((d, rank)))[0] for _ in range(K)])
+        return SubspaceMixture(cent.astype(np.float32), bases.astype(np.float32), 25.0, 6.0)
     if cfg == 3:   # 128 clusters, N(0,1) per dim around N(0,1) centres, min-max to [0,1]
         d = d or 960
         return Mixture(rng.standard_normal((128, d), np.float32), 1.0, "minmax")
@@ -113,6 +145,14 @@ def make_config(cfg: int, n: int | None = None, nq: int | None = None, d: int | 
     if with_gt:
         w.gt = ground_truth(base, q, min(gt_k, n), device=device)
     return w
+
+
+def training_queries(cfg: int, n: int, d: int | None = None) -> np.ndarray:
+    """Queries for training the learned entry: the config's mixture, seed 3003."""
+    mix = mixture_config(cfg, d)
+    if getattr(mix, "post", None) == "minmax":
+        raise ValueError("training queries are defined for configs 1, 2 and 4")
+    return mix.sample(n, SEED_TRAIN)
 
 
 def _torch_device(device):

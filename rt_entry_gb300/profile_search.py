@@ -1,0 +1,77 @@
+"""Profiling driver: the search kernel on the benchmark's index, few launches.
+
+    python -m rt_entry_gb300.profile_search [--nq 2000] [--precision 0|1|2] [--beam 64]
+                                            [--entry 1|2] [--rerank 0|1]
+
+Builds the 1M x 128 benchmark index (same generator, seeds and graph as
+bench.py), then launches the search kernel exactly twice on `nq` queries:
+one warm-up launch and one launch to capture, e.g.
+
+    ncu --set full --clock-control none -k regex:search_kernel -s 1 -c 1 \
+        -o prof python -m rt_entry_gb300.profile_search --nq 2000
+
+Prints the event-timed duration and the algorithmic bytes of the second
+launch so that ncu's DRAM bytes can be set against them.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+import torch
+
+import rt_entry_gb300 as r
+from rt_entry_gb300 import build as rbuild
+from rt_entry_gb300 import datasets as ds
+
+
+def algorithmic_bytes(cnt, d, L, R, k, elem_bytes=4, rerank=False):
+    E, X, D = cnt[:, 0].astype(np.float64), cnt[:, 1], cnt[:, 2]
+    b = 4 * d + 4 * L + elem_bytes * d * E + 4 * R * X + elem_bytes * d * D + 8 * k
+    if rerank:
+        b = b + 4 * d * L
+    return float(b.sum())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--nq", type=int, default=2000)
+    ap.add_argument("--precision", type=int, default=0)
+    ap.add_argument("--beam", type=int, default=64)
+    ap.add_argument("--width", type=int, default=1)
+    ap.add_argument("--entry", type=int, default=1)
+    ap.add_argument("--rerank", type=int, default=0)
+    a = ap.parse_args()
+    rbuild.build()
+    w = ds.make_config(2, nq=a.nq, with_gt=False, device="cuda")
+    idx = r.Index.from_arrays(w.base, w.graph).build_pca().build_kdtree(32, 0.2)
+    if a.entry == 2:
+        tr = ds.training_queries(2, 200_000)
+        idx.train_learned(tr)
+    qp = idx.project(torch.from_numpy(w.queries).cuda())
+    hits = idx.locate(qp)
+    p = r.default_params(beam=a.beam, k=10, search_width=a.width, precision=a.precision,
+                         rerank=a.rerank, entry_mode=a.entry)
+    idx.search_projected(qp, hits=hits if a.entry == 1 else None, params=p)  # warm-up launch
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    idx.search_projected(qp, hits=hits if a.entry == 1 else None, params=p)  # profiled launch
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    cnt = idx.counters(qp, hits=hits if a.entry == 1 else None, params=p)
+    s = {0: 4, 1: 2, 2: 1}[a.precision]
+    alg = algorithmic_bytes(cnt, w.base.shape[1], a.beam, w.graph.shape[1], 10, s, a.rerank == 1)
+    if a.precision == 2:
+        alg += 4.0 * (cnt[:, 0].sum() + cnt[:, 2].sum())  # per-vector scales
+    print(json.dumps({"nq": a.nq, "precision": a.precision, "beam": a.beam, "ms": ms,
+                      "alg_bytes": alg, "alg_gbs": alg / ms / 1e6,
+                      "mean_dist_evals": float(cnt[:, 2].mean()),
+                      "mean_expanded": float(cnt[:, 1].mean())}))
+
+
+if __name__ == "__main__":
+    main()

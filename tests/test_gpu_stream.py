@@ -1,0 +1,51 @@
+"""Uneven query streams: CUDA-graph replay of the query path (rte_batcher)
+and the parameter autotuner."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _index(n=8000, nq=1500, seed=41):
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    mix = ds.mixture_config(2)
+    base = mix.sample(n, seed)
+    q = mix.sample(nq, seed + 1)
+    graph = ds.knn_graph(base, 64)
+    idx = r.Index.from_arrays(base, graph).build_pca().build_kdtree(32, 0.2)
+    return idx, base, q
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_batcher_equals_direct_search_for_every_batch_size(lib, cuda, prec):
+    import torch
+
+    import rt_entry_gb300 as r
+    idx, base, q = _index()
+    p = r.default_params(beam=64, k=10, precision=prec, rerank=int(prec > 0))
+    want, wd = idx.search(q, params=p)
+    b = idx.batcher(1024, params=p)
+    assert b.k == 10
+    qt = torch.from_numpy(q).cuda()
+    for s, e in [(0, 1), (1, 3), (3, 131), (131, 1024), (1024, 1500), (0, 7)]:
+        ids, dd = b.search(q[s:e])                      # host in, host out
+        assert np.array_equal(ids, want[s:e]) and np.array_equal(dd, wd[s:e]), (s, e)
+        ti, td = b.search(qt[s:e])                      # device in, device out
+        assert np.array_equal(ti.cpu().numpy(), want[s:e]), (s, e)
+    with pytest.raises(r.RteError):
+        b.search(q[:1025])
+    b.close()
+
+
+def test_autotune_meets_the_recall_target(lib, cuda):
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    idx, base, q = _index()
+    gt = ds.ground_truth(base, q[:600], 10)
+    p, rep = idx.autotune(q[:600], gt, k=10, target_recall=0.9)
+    assert rep["evaluated"] >= 10
+    assert rep["met_target"] == 1 and rep["recall"] >= 0.9
+    ids, _ = idx.search(q[:600], params=p)
+    assert ds.recall_at(ids, gt, 10) == pytest.approx(rep["recall"], abs=1e-6)
+    assert p.beam in (32, 64, 128, 256) and p.bloom_words in (512, 2048, 8192)
