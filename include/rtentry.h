@@ -139,6 +139,28 @@ rte_status rte_search_projected(rte_index* idx, const float* projected, const in
                                 int64_t nq, const rte_search_params* params, int32_t* out_ids,
                                 float* out_dists, void* stream);
 
+/* rte_search_projected without any memory allocation.  No counterpart in the
+ * reference.  Meant for callers that cannot let a library allocate device
+ * memory once they are running: a server that reserves all of its GPU
+ * memory at start-up and treats a later cudaMalloc as a failure (it can
+ * stall on a device-wide synchronisation or fail under memory pressure), or
+ * a framework whose allocator owns the device.  Differences from
+ * rte_search_projected:
+ *   - every pointer must be device memory; entry_mode random or kd-tree;
+ *   - at most RTE_NOALLOC_MAX_QUERIES queries per call (RTE_EINVAL beyond);
+ *   - its scratch (each query's leaf and the search's work counter, about
+ *     256 KB) is one fixed array inside the library that every GPU loading
+ *     the library holds until the process exits.  The first call on a
+ *     device looks up that array's device address, so make the first call
+ *     before any stream capture.  All calls share the one array: calls that
+ *     overlap on the GPU (other streams, other threads) race on it, so the
+ *     caller must not let them overlap. */
+#define RTE_NOALLOC_MAX_QUERIES 65536
+rte_status rte_search_projected_noalloc(rte_index* idx, const float* projected,
+                                        const int32_t* hits, int64_t nq,
+                                        const rte_search_params* params, int32_t* out_ids,
+                                        float* out_dists, void* stream);
+
 /* ---- uneven query streams (spec form 2; no reference counterpart:
  * the reference launches each stage separately and synchronises the device
  * after each, graph.cu:254-337) ----

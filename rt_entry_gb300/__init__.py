@@ -31,7 +31,7 @@ EXPORTS = (
     "rte_get_kdtree", "rte_index_save", "rte_index_load_dir", "rte_index_free", "rte_last_error",
     "rte_kdtree_build_host", "rte_sym_eig_host", "rte_get_search_base_lowp", "rte_gemm_bf16",
     "rte_default_train_params", "rte_learned_train", "rte_learned_predict", "rte_mlp_grad_check",
-    "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
+    "rte_search_projected_noalloc", "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
     "rte_batcher_free", "rte_autotune",
 )
 
@@ -126,6 +126,7 @@ def load_library(path: str = LIB_PATH):
         "rte_learned_train": ([P, P, i64, ctypes.POINTER(TrainParams), ctypes.POINTER(TrainReport)], i32),
         "rte_learned_predict": ([P, P, i64, P, P], i32),
         "rte_mlp_grad_check": ([P, P, i32, i32, i32, i32] + [P] * 13, i32),
+        "rte_search_projected_noalloc": ([P, P, P, i64, SP, P, P, P], i32),
         "rte_batcher_create": ([P, i64, SP, PP], i32),
         "rte_batcher_search": ([P, P, i64, P, P, P], i32),
         "rte_batcher_k": ([P], i32),

@@ -1,0 +1,133 @@
+// noalloc.cu -- a search entry point that allocates no memory.
+//
+// Some callers cannot let a library allocate device memory once they are
+// running: a serving process that reserves all of its GPU memory at start-up
+// and treats any later cudaMalloc as a failure (an allocation can stall on
+// a device-wide synchronisation or fail under memory pressure in the middle
+// of a request), or a host framework whose own allocator owns the device and
+// forbids third-party libraries to allocate behind its back.  For them
+// rte_search_projected_noalloc runs the entry-point location and the beam
+// search with every buffer supplied: the caller passes the inputs and the
+// outputs, and the only scratch the two kernels need -- the leaf of each
+// query and the work-queue counter of the persistent search -- lives in the
+// file-scope array below, reserved once when the library is loaded on a
+// device and kept until the process exits.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "index_impl.h"
+#include "index_kernels.h"
+#include "search_dispatch.h"
+
+namespace rte {
+rte_status search_plan(const rte_index* x, const rte_search_params* prm, int64_t nq, int* L, int* k,
+                       int* NL, int* NB, int* wpb, int* grid, size_t* smem);
+}  // namespace rte
+
+using namespace rte;
+
+namespace {
+
+// Largest batch one call accepts (RTE_NOALLOC_MAX_QUERIES in rtentry.h).
+constexpr int kMaxQueries = 65536;
+
+// [0, 256): the search's work counter (first 4 bytes); [256, ...): hits.
+struct NoallocScratch {
+  unsigned int counter[64];
+  int32_t hits[kMaxQueries];
+};
+
+// Every GPU that loads the library holds this array until the process exits.
+static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
+
+// Host code cannot use the symbol as a device address: it is a host-side
+// stand-in.  The device address comes from cudaGetSymbolAddress, looked up
+// once per device with that device current, and cached.
+constexpr int kMaxDevices = 64;
+std::mutex g_lock;
+NoallocScratch* g_addr[kMaxDevices] = {};
+
+rte_status scratch_for_device(int dev, NoallocScratch** out) {
+  if (dev < 0 || dev >= kMaxDevices) return fail(RTE_EINVAL, "device index out of range");
+  std::lock_guard<std::mutex> lk(g_lock);
+  if (!g_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      return fail(RTE_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_addr[dev] = static_cast<NoallocScratch*>(p);
+  }
+  *out = g_addr[dev];
+  return RTE_OK;
+}
+
+}  // namespace
+
+extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* projected,
+                                                   const int32_t* hits, int64_t nq,
+                                                   const rte_search_params* params,
+                                                   int32_t* out_ids, float* out_dists,
+                                                   void* stream) {
+  clear_error();
+  if (!x || !params) return fail(RTE_EINVAL, "NULL argument");
+  if (nq < 0) return fail(RTE_EINVAL, "nq < 0");
+  if (nq > kMaxQueries)
+    return fail(RTE_EINVAL, "rte_search_projected_noalloc takes at most " +
+                                std::to_string(kMaxQueries) + " queries per call");
+  if (params->entry_mode != RTE_ENTRY_RANDOM && params->entry_mode != RTE_ENTRY_KDTREE)
+    return fail(RTE_EINVAL, "rte_search_projected_noalloc supports random and kd-tree entries only");
+  if (nq == 0) return RTE_OK;
+  if (!projected || !out_ids) return fail(RTE_EINVAL, "NULL argument");
+  // inputs and outputs must already be device memory: copying host data
+  // would need staging buffers
+  if (!is_device_ptr(projected) || !is_device_ptr(out_ids) ||
+      (out_dists && !is_device_ptr(out_dists)) || (hits && !is_device_ptr(hits)))
+    return fail(RTE_EINVAL, "rte_search_projected_noalloc takes device pointers only");
+  DeviceGuard guard(x->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  int L, k, NL, NB, wpb, grid;
+  size_t smem;
+  rte_status s = search_plan(x, params, nq, &L, &k, &NL, &NB, &wpb, &grid, &smem);
+  if (s != RTE_OK) return s;
+  NoallocScratch* scr = nullptr;
+  s = scratch_for_device(x->device, &scr);
+  if (s != RTE_OK) return s;
+  const int32_t* h = hits;
+  if (params->entry_mode == RTE_ENTRY_KDTREE && !h) {
+    RTE_CUDA(launch_locate(x->d_nodes.p, projected, nq, x->search_dim, scr->hits, st));
+    h = scr->hits;
+  }
+  // the array keeps the previous call's contents: the counter must restart at 0
+  RTE_CUDA(cudaMemsetAsync(scr->counter, 0, sizeof(unsigned int), st));
+  SearchArgs a{};
+  a.base = x->il32.p;
+  a.base_bf16 = x->il16.p;
+  a.base_fp8 = x->il8.p;
+  a.fp8_scale = x->scale8.p;
+  a.queries = projected;
+  a.graph = x->graph.p;
+  a.leaf_pids = x->has_kdtree ? x->d_pids.p : nullptr;
+  a.hits = h;
+  a.hits2 = nullptr;
+  a.out_ids = out_ids;
+  a.out_dists = out_dists;
+  a.counters = nullptr;
+  a.work = scr->counter;
+  a.np = (int)x->np;
+  a.d = x->search_dim;
+  a.qstride = x->search_dim;
+  a.nq = (int)nq;
+  a.R = x->degree;
+  a.W = params->search_width;
+  a.k = k;
+  a.max_iter = params->max_iter;
+  a.bloom_words = params->bloom_words;
+  a.bloom_hashes = params->bloom_hashes;
+  a.leaf_cap = x->has_kdtree ? x->kd.cap : 1;
+  a.entry_mode = params->entry_mode;
+  a.rerank = params->rerank;
+  a.n_leaves = x->has_kdtree ? (int)x->kd.n_leaves : 1;
+  RTE_CUDA(launch_search(a, x->C, NL, NB, params->precision, wpb, grid, smem, st));
+  return RTE_OK;
+}
