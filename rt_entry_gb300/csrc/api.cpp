@@ -161,7 +161,7 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
   pl.L = next_pow2(prm->beam);  // graph.cu:53
   pl.k = prm->k == 0 ? pl.L : prm->k;  // graph.cu:54
   if (pl.k < 0 || pl.k > pl.L) return fail(RTE_EINVAL, "k must be in [1, beam] (topk <= n_candidates)");
-  if (pl.L < 32 || pl.L > 256) return fail(RTE_EINVAL, "beam must round to 32..256");
+  if (pl.L < 16 || pl.L > 256) return fail(RTE_EINVAL, "beam must round to 16..256");
   if (x->degree < 32) return fail(RTE_EINVAL, "graph degree must be >= 32 for the warp kernel");
   if (prm->search_width <= 0) return fail(RTE_EINVAL, "search_width must be >= 1");
   const int B = prm->search_width * x->degree;
@@ -179,7 +179,7 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
     return fail(RTE_ESTATE, "kd-tree entries requested before rte_build_kdtree");
   if (!search_chunks_supported(x->C))
     return fail(RTE_EINVAL, "search dimension " + std::to_string(x->search_dim) + " has no kernel instantiation");
-  pl.NL = pl.L / 32;
+  pl.NL = pl.L / 32;  // 0 selects the 16-slot pool
   pl.NB = B / 32;
   pl.prec = prm->precision;
   // per warp: the bloom filter plus the compaction buffers (ids, distances)

@@ -3,8 +3,9 @@
 // Computes exactly what the reference's GraphSearchKernel computes
 // (graph_search.cuh:56-1964, one 64-thread block per query), reorganised for
 // one warp per query:
-//   * the pool (L = 32*NL slots) and the batch (B = 32*NB slots) live in
-//     registers: slot p sits in lane p%32, register p/32.  The reference's
+//   * the pool (L = 32*NL slots, or 16 slots for NL = 0) and the batch
+//     (B = 32*NB slots) live in registers: slot p sits in lane p%32,
+//     register p/32.  The reference's
 //     comparator network (bitonic batch sort, pool/batch merge, half-cleaner,
 //     graph_search.cuh:888-957 and :1424-1493) runs on those registers,
 //     across lanes through shuffles and inside a lane for distances >= 32;
@@ -114,13 +115,20 @@ __device__ __forceinline__ void cx_regs(float& da, int& ia, float& db, int& ib, 
   }
 }
 
-// Bitonic sort of 32*NB slots (graph_search.cuh:888-919).  With DESC_FINAL
-// the pair (a, a+sub) is descending when a's 2*step block index is even, so
-// the result is descending, as the reference sorts its batch; otherwise the
-// directions are mirrored and the result is ascending.
-template <int NB, bool DESC_FINAL = true>
+// Pool geometry: NL registers of 32 slots each, or NL == 0 for a 16-slot pool
+// (beam 16) held in lanes 0..15 of one register; lanes 16..31 of that
+// register keep (MAX, np) padding that no step ever reads back.
+__host__ __device__ constexpr int pool_slots(int NL) { return NL == 0 ? 16 : 32 * NL; }
+__host__ __device__ constexpr int pool_regs(int NL) { return NL == 0 ? 1 : NL; }
+
+// Bitonic sort of N slots (graph_search.cuh:888-919), N = 32*NB by default or
+// 16 for the one-register beam-16 pool.  With DESC_FINAL the pair (a, a+sub)
+// is descending when a's 2*step block index is even, so the result is
+// descending, as the reference sorts its batch; otherwise the directions are
+// mirrored and the result is ascending.
+template <int NB, bool DESC_FINAL = true, int N = 32 * NB>
 __device__ __forceinline__ void sort_batch_desc(float (&d)[NB], int (&id)[NB], int lane) {
-  constexpr int B = 32 * NB;
+  constexpr int B = N;
 #pragma unroll
   for (int step = 1; step <= B / 2; step <<= 1) {
 #pragma unroll
@@ -148,32 +156,48 @@ __device__ __forceinline__ void sort_batch_desc(float (&d)[NB], int (&id)[NB], i
 // :1454-1493).  Pool slot L-n+i meets batch slot B-n+i (n = min(L,B)); both
 // are in the same lane.  The main loop skips a batch slot holding MAX.
 template <int NL, int NB>
-__device__ __forceinline__ void merge_pool(float (&pd)[NL], int (&pi)[NL], const float (&bd)[NB],
-                                           const int (&bi)[NB], bool skip_max, int lane) {
-  constexpr int NC = NL < NB ? NL : NB;
-#pragma unroll
-  for (int m = 0; m < NC; ++m) {
-    const int pr = NL - NC + m, br = NB - NC + m;
-    bool take = pd[pr] > bd[br];
-    if (skip_max && bd[br] == kMaxDist) take = false;
+__device__ __forceinline__ void merge_pool(float (&pd)[pool_regs(NL)], int (&pi)[pool_regs(NL)],
+                                           const float (&bd)[NB], const int (&bi)[NB], bool skip_max,
+                                           int lane) {
+  if constexpr (NL == 0) {
+    // 16-slot pool: pool slot i (lane i) meets batch slot B-16+i, which is
+    // lane 16+i of the last batch register.
+    const float od = __shfl_down_sync(kFull, bd[NB - 1], 16);
+    const int oi = __shfl_down_sync(kFull, bi[NB - 1], 16);
+    bool take = lane < 16 && pd[0] > od;
+    if (skip_max && od == kMaxDist) take = false;
     if (take) {
-      pd[pr] = bd[br];
-      pi[pr] = bi[br];
+      pd[0] = od;
+      pi[0] = oi;
     }
-  }
-  constexpr int L = 32 * NL;
 #pragma unroll
-  for (int sub = L / 2; sub >= 1; sub >>= 1) {
-    if (sub >= 32) {
-      const int rs = sub >> 5;
+    for (int sub = 8; sub >= 1; sub >>= 1) cx_lanes(pd[0], pi[0], sub, false, lane);
+  } else {
+    constexpr int NC = NL < NB ? NL : NB;
 #pragma unroll
-      for (int j = 0; j < NL; ++j) {
-        if (j & rs) continue;
-        cx_regs(pd[j], pi[j], pd[j + rs], pi[j + rs], false);
+    for (int m = 0; m < NC; ++m) {
+      const int pr = NL - NC + m, br = NB - NC + m;
+      bool take = pd[pr] > bd[br];
+      if (skip_max && bd[br] == kMaxDist) take = false;
+      if (take) {
+        pd[pr] = bd[br];
+        pi[pr] = bi[br];
       }
-    } else {
+    }
+    constexpr int L = 32 * NL;
 #pragma unroll
-      for (int j = 0; j < NL; ++j) cx_lanes(pd[j], pi[j], sub, false, lane);
+    for (int sub = L / 2; sub >= 1; sub >>= 1) {
+      if (sub >= 32) {
+        const int rs = sub >> 5;
+#pragma unroll
+        for (int j = 0; j < NL; ++j) {
+          if (j & rs) continue;
+          cx_regs(pd[j], pi[j], pd[j + rs], pi[j + rs], false);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < NL; ++j) cx_lanes(pd[j], pi[j], sub, false, lane);
+      }
     }
   }
 }
@@ -314,13 +338,14 @@ __device__ __forceinline__ int batch_distances(const SearchArgs& a, const float 
 // (graph_helper.cu:146-213), which recomputes FP32 L2 and std::sorts.
 template <int C, int NL>
 __device__ __forceinline__ void rerank_pool(const SearchArgs& a, const float (&qv)[C],
-                                            float (&pd)[NL], int (&pi)[NL], int* s_ids,
-                                            float* s_dist, int lane) {
+                                            float (&pd)[pool_regs(NL)], int (&pi)[pool_regs(NL)],
+                                            int* s_ids, float* s_dist, int lane) {
+  constexpr int PR = pool_regs(NL);
   const unsigned lt = (1u << lane) - 1u;
-  int kidx[NL];
+  int kidx[PR];
   int n = 0;
 #pragma unroll
-  for (int j = 0; j < NL; ++j) {
+  for (int j = 0; j < PR; ++j) {
     pi[j] = pi[j] < 0 ? -pi[j] : pi[j];
     const bool v = pi[j] < a.np;
     const unsigned m = __ballot_sync(kFull, v);
@@ -332,15 +357,16 @@ __device__ __forceinline__ void rerank_pool(const SearchArgs& a, const float (&q
   distances<C, kPrecF32>(a, qv, s_ids, s_dist, n, lane);
   __syncwarp();
 #pragma unroll
-  for (int j = 0; j < NL; ++j) pd[j] = kidx[j] >= 0 ? s_dist[kidx[j]] : kMaxDist;
+  for (int j = 0; j < PR; ++j) pd[j] = kidx[j] >= 0 ? s_dist[kidx[j]] : kMaxDist;
   __syncwarp();
-  sort_batch_desc<NL, false>(pd, pi, lane);
+  sort_batch_desc<PR, false, pool_slots(NL)>(pd, pi, lane);
 }
 
 template <int C, int NL, int NB, int PREC>
 __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& bloom, int* s_ids,
                              float* s_dist) {
-  constexpr int L = 32 * NL;
+  constexpr int L = pool_slots(NL);
+  constexpr int PR = pool_regs(NL);  // pool registers
   constexpr int B = 32 * NB;
   const int np = a.np;
   const int R = a.R;
@@ -354,10 +380,10 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     qv[c] = dim < a.d ? __ldg(a.queries + (size_t)q * a.qstride + dim) : 0.0f;
   }
 
-  float pd[NL];
-  int pi[NL];
+  float pd[PR];
+  int pi[PR];
 #pragma unroll
-  for (int j = 0; j < NL; ++j) {
+  for (int j = 0; j < PR; ++j) {
     pd[j] = kMaxDist;
     pi[j] = np;
   }
@@ -409,7 +435,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
   }
 
   // ---- main loop (graph_search.cuh:961-1532) ----
-  uint32_t tmp_flag = 0xFFFFFFFFu;  // (1 << min(L,32)) - 1 with L >= 32 (:969)
+  uint32_t tmp_flag = L >= 32 ? 0xFFFFFFFFu : ((1u << L) - 1u);  // (1 << min(L,32)) - 1 (:969)
   int iteration = 0;
   bool cz = false;  // this lane's check_zero (:967)
   int hash_iteration = 0;
@@ -417,8 +443,8 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
 
   auto scan = [&](int chunk) -> uint32_t {  // :1019-1028, :1495-1510
     bool pred = false;
-    if (chunk < NL) {
-      const int id = pick<NL>(pi, chunk);
+    if (chunk < PR && (L >= 32 || lane < L)) {
+      const int id = pick<PR>(pi, chunk);
       if (id > 0 && id < np) {
         pred = true;
       } else if (id == 0 && !cz) {
@@ -440,10 +466,10 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     while (nsel < a.W && tmp_flag != 0) {
       const int pos = __ffs(tmp_flag) - 1;
       const int chunk = iteration;
-      const int v = __shfl_sync(kFull, pick<NL>(pi, chunk), pos);
+      const int v = __shfl_sync(kFull, pick<PR>(pi, chunk), pos);
       if (lane == pos) {
 #pragma unroll
-        for (int j = 0; j < NL; ++j)
+        for (int j = 0; j < PR; ++j)
           if (j == chunk) pi[j] = -pi[j];
       }
       tmp_flag &= ~(1u << pos);
@@ -453,7 +479,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
         if (s == nsel) nodes[s] = node;
       nsel++;
       if (nsel == a.W) break;
-      while (tmp_flag == 0 && iteration < NL) {
+      while (tmp_flag == 0 && iteration < PR) {
         iteration++;
         tmp_flag = scan(iteration);
       }
@@ -503,7 +529,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
 
     bool any = false;
 #pragma unroll 1
-    for (iteration = 0; iteration < NL; iteration++) {
+    for (iteration = 0; iteration < PR; iteration++) {
       tmp_flag = scan(iteration);
       if (tmp_flag != 0) {
         any = true;
@@ -515,7 +541,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
       bloom.clear(lane);
       __syncwarp();
 #pragma unroll
-      for (int j = 0; j < NL; ++j) {
+      for (int j = 0; j < PR; ++j) {
         const int id = pi[j] < 0 ? -pi[j] : pi[j];
         if (id < np) bloom.add((uint32_t)id);
       }
@@ -531,7 +557,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
 
   // ---- output (:1959-1963) ----
 #pragma unroll
-  for (int j = 0; j < NL; ++j) {
+  for (int j = 0; j < PR; ++j) {
     const int i = (j << 5) + lane;
     if (i < a.k) {
       a.out_ids[(size_t)q * a.k + i] = pi[j] < 0 ? -pi[j] : pi[j];
@@ -553,7 +579,7 @@ __global__ void __launch_bounds__(256, (C <= 4 ? 4 : 2)) search_kernel(SearchArg
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   constexpr int B = 32 * NB;
-  constexpr int S = B > 32 * NL ? B : 32 * NL;  // compaction slots per warp
+  constexpr int S = B > pool_slots(NL) ? B : pool_slots(NL);  // compaction slots per warp
   const int per_warp = a.bloom_words + 2 * S;
   uint32_t* wbase = smem + (size_t)wib * per_warp;
   Bloom bloom;

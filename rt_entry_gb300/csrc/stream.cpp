@@ -191,7 +191,7 @@ extern "C" rte_status rte_autotune(rte_index* x, const float* queries, int64_t n
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int beams[] = {32, 64, 128, 256};
+  const int beams[] = {16, 32, 64, 128, 256};
   const int widths[] = {1, 2, 4};
   const int blooms[] = {512, 2048, 8192};
   const int wpbs[] = {4, 8};

@@ -73,6 +73,12 @@ def test_learned_entry_trains_and_searches(lib, orc, cuda):
                           hits2=kd)
     assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
     assert np.array_equal(dd, od)
+    # beam 16: eight entries from each leaf
+    ids, dd = idx.search_projected(qp, beam=16, k=16, entry_mode=r.ENTRY_LEARNED)
+    oids, od = orc.search(pb, qp, graph, L=16, k=16, entry_mode=2, leaf_pids=pids, hits=learned,
+                          hits2=kd)
+    assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
+    assert np.array_equal(dd, od)
     # what the model gains: recall at a small beam with vs without it
     rk, _ = idx.search(q, beam=32, k=10)
     rl, _ = idx.search(q, beam=32, k=10, entry_mode=r.ENTRY_LEARNED)

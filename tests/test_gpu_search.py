@@ -73,6 +73,10 @@ SWEEP = [
     (128, True, 64, 32, 1, 32, 5, 1, 100),      # tiny filter: many false positives
     (128, False, 64, 64, 1, 512, 3, 1, 7),      # stops at max_iter
     (128, True, 32, 64, 2, 1024, 1, 0, 100),
+    (128, True, 64, 16, 1, 512, 3, 1, 100),     # beam 16: half-warp pool
+    (32, False, 32, 16, 1, 512, 3, 0, 100),
+    (128, False, 32, 16, 2, 1024, 3, 1, 100),
+    (64, True, 32, 16, 1, 32, 4, 1, 5),
 ]
 
 
@@ -184,9 +188,10 @@ def test_locate_matches_oracle_including_faces(lib, orc, cuda):
     assert (want == 0).any()  # misses fall back to leaf 0
 
 
+@pytest.mark.parametrize("L", [64, 16])
 @pytest.mark.parametrize("prec", [1, 2])
 @pytest.mark.parametrize("rerank", [0, 1])
-def test_low_precision_paths_match_oracle(lib, orc, cuda, prec, rerank):
+def test_low_precision_paths_match_oracle(lib, orc, cuda, prec, rerank, L):
     from rt_entry_gb300 import datasets as ds
     base, q = _mixture(3000, 200, 128, False, seed=31 + prec)
     graph = ds.knn_graph(base, 64)
@@ -201,8 +206,8 @@ def test_low_precision_paths_match_oracle(lib, orc, cuda, prec, rerank):
     else:
         rel = np.abs(low - base) / np.maximum(np.abs(base).max(1, keepdims=True), 1e-9)
         assert rel.max() <= 2 ** -4 + 1e-6  # E4M3: 3 mantissa bits, scale = max|x|/448
-    ids, dd = idx.search_projected(q, beam=64, k=64, precision=prec, rerank=rerank)
-    oids, od = orc.search(low, q, graph, L=64, k=64, leaf_pids=pids, hits=hits,
+    ids, dd = idx.search_projected(q, beam=L, k=L, precision=prec, rerank=rerank)
+    oids, od = orc.search(low, q, graph, L=L, k=L, leaf_pids=pids, hits=hits,
                           rerank_base=base if rerank else None)
     assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
     assert np.array_equal(dd, od)
@@ -217,7 +222,7 @@ def test_parameter_errors(lib, cuda):
         idx.search_projected(q, beam=64, k=10)  # kd-tree entries before the kd-tree
     assert e.value.status == r.RTE_ESTATE
     idx.build_kdtree(32, 0.2)
-    for kw in (dict(beam=64, k=65), dict(beam=16, k=10), dict(beam=512, k=10),
+    for kw in (dict(beam=64, k=65), dict(beam=8, k=4), dict(beam=16, k=17), dict(beam=512, k=10),
                dict(beam=64, k=10, bloom_words=1000), dict(beam=64, k=10, bloom_hashes=11),
                dict(beam=64, k=10, search_width=3), dict(beam=64, k=10, precision=7),
                dict(beam=64, k=10, max_iter=-1)):
