@@ -182,7 +182,12 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
   // ---- entry phase (:479-959) ----
   uint32_t seed[64];
   for (int t = 0; t < 64; ++t) seed[t] = (uint32_t)(qid * 64 + t);  // :64
-  const int n_entries = L;
+  // Entry mode 2 (no reference counterpart): every point of the first leaf,
+  // then every point of the second leaf (hit2), max(L, both) entry slots.
+  const bool two = A.entry_mode == 2 && hit2 >= 0 && hit2 != hit;
+  const int n_first = A.leaf_cap;
+  const int n_second = two ? A.leaf_cap : 0;
+  const int n_entries = A.entry_mode == 2 ? std::max(L, n_first + n_second) : L;  // :479
   const int n_ebatch = (n_entries + B - 1) / B;
   for (int it = 0; it < n_ebatch; ++it) {
     for (int i = 0; i < B; ++i) {
@@ -192,11 +197,7 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
         if (A.entry_mode == 0) {
           id = (int)lcg_next(seed[i % 64], (uint32_t)np);
         } else {
-          // entry.cu:60-69.  Entry mode 2 (no reference counterpart): the first
-          // leaf's points, at most half the beam, then the second leaf's (hit2).
-          const bool two = A.entry_mode == 2 && hit2 >= 0 && hit2 != hit;
-          const int n_first = two ? std::min(A.leaf_cap, L / 2) : A.leaf_cap;
-          const int n_second = two ? std::min(A.leaf_cap, L - n_first) : 0;
+          // entry.cu:60-69 (mode 1: the leaf's points, then padding)
           if (j < n_first)
             id = A.leaf_pids[(int64_t)hit * A.leaf_cap + j];
           else if (j < n_first + n_second)
@@ -221,8 +222,8 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
   }
 
   // ---- main loop (:961-1532) ----
-  int n_first = std::min(std::min(L, 32), n_entries);
-  uint32_t tmp_flag = n_first >= 32 ? 0xFFFFFFFFu : ((1u << n_first) - 1u);  // :969
+  const int n_flag = std::min(std::min(L, 32), n_entries);
+  uint32_t tmp_flag = n_flag >= 32 ? 0xFFFFFFFFu : ((1u << n_flag) - 1u);  // :969
   uint32_t check_zero = 0;  // bit l = lane l's check_zero (H5)
   int iteration = 0;
   bool flag_all = true;

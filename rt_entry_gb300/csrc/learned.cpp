@@ -292,7 +292,7 @@ extern "C" rte_status rte_learned_train(rte_index* x, const float* train_queries
   if (s != RTE_OK) return s;
   std::vector<int32_t> ids(n), leaf_of(x->np, 0), labels(n);
   RTE_CUDA(cudaMemcpy(ids.data(), top.p, n * 4, cudaMemcpyDeviceToHost));
-  for (int64_t l = 0; l < C; ++l)
+  for (int64_t l = 0; l < x->kd.n_leaves; ++l)
     for (int j = 0; j < x->kd.cap; ++j) {
       const int32_t p = x->kd.pids[l * x->kd.cap + j];
       if (p < x->np) leaf_of[p] = (int32_t)l;

@@ -397,24 +397,25 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
   int hit = a.entry_mode != 0 ? __ldg(a.hits + q) : 0;
   if (hit < 0 || hit >= a.n_leaves) hit = 0;
   const int32_t* lp = a.leaf_pids + (size_t)hit * a.leaf_cap;
-  // learned entries: the proposed leaf's points, then the kd-tree leaf's
+  // learned entries (mode 2): every point of the proposed leaf, then every
+  // point of the kd-tree leaf, max(L, both leaves) entry slots in all; the
+  // pool keeps the best L of them.  Modes 0 and 1 have L entry slots (:479).
   int hit2 = a.entry_mode == 2 ? __ldg(a.hits2 + q) : -1;
   if (hit2 >= a.n_leaves || hit2 == hit) hit2 = -1;
   const int32_t* lp2 = a.leaf_pids + (size_t)(hit2 < 0 ? 0 : hit2) * a.leaf_cap;
-  // entry slots: the first leaf's points (at most half the beam when a second
-  // leaf follows), then the second leaf's points
-  const int n_first = hit2 >= 0 ? min(a.leaf_cap, L / 2) : a.leaf_cap;
-  const int n_second = hit2 >= 0 ? min(a.leaf_cap, L - n_first) : 0;
+  const int n_first = a.leaf_cap;
+  const int n_second = hit2 >= 0 ? a.leaf_cap : 0;
+  const int n_entries = a.entry_mode == 2 ? max(L, n_first + n_second) : L;
   uint32_t seed0 = (uint32_t)q * 64u + (uint32_t)lane;  // reference thread `lane`
   uint32_t seed1 = seed0 + 32u;                           // reference thread `lane + 32`
-  constexpr int kEntryBatches = (L + B - 1) / B;
+  const int n_ebatch = (n_entries + B - 1) / B;
 #pragma unroll 1
-  for (int it = 0; it < kEntryBatches; ++it) {
+  for (int it = 0; it < n_ebatch; ++it) {
 #pragma unroll
     for (int j = 0; j < NB; ++j) {
       const int pos = it * B + (j << 5) + lane;
       int id = np;
-      if (pos < L) {
+      if (pos < n_entries) {
         if (a.entry_mode == 0) {
           uint32_t& s = (j & 1) ? seed1 : seed0;
           s = s * 1103515245u + 12345u;

@@ -65,6 +65,8 @@ def test_learned_entry_trains_and_searches(lib, orc, cuda):
     learned = idx.learned_leaves(qp)
     kd = idx.locate(qp)
     assert learned.shape == kd.shape and ((learned >= 0) & (learned < idx.info.n_leaves)).all()
+    # the predictions spread over the tree (labels come from every leaf)
+    assert len(np.unique(learned)) > 100
     # the learned search is bit-exact with the oracle given the same two leaves
     pb = idx.search_base()
     _, _, pids = idx.kdtree()
@@ -85,3 +87,8 @@ def test_learned_entry_trains_and_searches(lib, orc, cuda):
     rec_kd = ds.recall_at(rk, gt, 10)
     rec_l = ds.recall_at(rl, gt, 10)
     assert rec_l >= rec_kd - 0.01, (rec_l, rec_kd)
+    # the model's leaf alone, without the kd-tree leaf, is a usable entry
+    # (a model mapped to the wrong leaves scores near zero here)
+    ro, _ = idx.search_projected(qp, hits=learned, beam=32, k=10, entry_mode=r.ENTRY_KDTREE)
+    rec_o = ds.recall_at(ro, gt, 10)
+    assert rec_o >= 0.85, (rec_o, rec_kd)
