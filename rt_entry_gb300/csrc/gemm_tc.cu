@@ -1,18 +1,24 @@
 // gemm_tc.cu -- BF16 x BF16 -> FP32 GEMM on the 5th-generation tensor cores.
 //
-// One CTA of 4 warps computes a 128 x 128 output tile:
-//   * warp 0 / lane 0 streams 128 x 64 tiles of A and B into shared memory
-//     with TMA (cp.async.bulk.tensor, 128-byte swizzle) through a 4-stage
-//     ring guarded by mbarriers;
-//   * warp 1 / lane 0 issues tcgen05.mma (M=128, N=128, K=16, BF16 inputs,
-//     FP32 accumulation) into a 128-column TMEM accumulator and releases
-//     each ring slot with tcgen05.commit;
-//   * all four warps then read their 32 accumulator rows with tcgen05.ld and
-//     apply the fused epilogue.
+// A persistent grid (one CTA of 10 warps per SM) splits the 128 x 128 output
+// tiles into contiguous ranges, row-block major:
+//   * warp 8 / lane 0 streams 128 x 64 tiles into shared memory with TMA
+//     (cp.async.bulk.tensor, 128-byte swizzle) through an mbarrier ring.
+//     When K <= 256 the A block is loaded once per row block and stays
+//     resident while 7 stages of B tiles stream; otherwise 5 stages carry
+//     both;
+//   * warp 9 / lane 0 issues tcgen05.mma (M=128, N=128, K=16, BF16 inputs,
+//     FP32 accumulation) into one of two 128-column TMEM accumulators, so the
+//     next tile's MMAs overlap the epilogue of the previous one;
+//   * warps 0-7 (two per TMEM lane quarter, each on half of the columns)
+//     read the accumulator with wide tcgen05.ld, hand it back, and apply the
+//     fused epilogue: a running argmax kept in registers across tiles, or
+//     stores staged through shared memory so each warp writes 128-byte row
+//     segments (coalesced).
 // Every mbarrier wait is bounded: when one runs out the kernel records an
-// error code in *err, stops issuing work, lets the copies already in flight
-// land, frees its TMEM and returns, so a fault in the pipeline cannot hang
-// the GPU.
+// error code in *err, raises an abort flag the other roles poll, lets the
+// copies already in flight land, frees its TMEM and returns, so a fault in
+// the pipeline cannot hang the GPU.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -25,10 +31,24 @@ namespace rte {
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 4;
-constexpr int A_BYTES = BM * BK * 2;
-constexpr int B_BYTES = BN * BK * 2;
-constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + 1024 /*align*/ + 256 /*barriers*/;
+constexpr int BM = 128, BN = 128, BK = 64;
+constexpr int A_BYTES = BM * BK * 2;  // one 128 x 64 chunk of A
+constexpr int B_BYTES = BN * BK * 2;  // one 128 x 64 chunk of B
+constexpr int RING_BYTES = 11 * A_BYTES;
+// resident A (K <= 256): 4 A chunks + 7 B stages; streamed: 5 stages of A + B
+constexpr int kResidentChunks = 4;
+constexpr int kResidentK = kResidentChunks * BK;
+constexpr int kStagesResident = (RING_BYTES - kResidentChunks * A_BYTES) / B_BYTES;
+constexpr int kStagesStreamed = RING_BYTES / (A_BYTES + B_BYTES);
+constexpr int kMaxStages = kStagesResident;
+constexpr int kChunk = 32;                // accumulator columns per TMEM load
+constexpr int kStageLd = kChunk + 4;      // staging row pitch (floats): conflict-free v4 access
+constexpr int kEpiWarps = 8;             // two per TMEM lane quarter, one per column half
+constexpr int kHalf = BN / 2;
+constexpr int STAGE_BYTES = kEpiWarps * 32 * kStageLd * 4;
+constexpr int SMEM_BYTES = RING_BYTES + STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+constexpr int kProducerWarp = kEpiWarps, kMmaWarp = kEpiWarps + 1;
+constexpr int kThreads = 32 * (kEpiWarps + 2);
 constexpr long long kWaitLimit = 1ll << 24;  // try_wait rounds before giving up (~seconds)
 
 // Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
@@ -74,12 +94,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait; returns false (and records `code`) when the limit runs out.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
-  for (long long i = 0; i < kWaitLimit; ++i)
+// Bounded wait; returns false (and records `code`) when the limit runs out
+// or another role of the CTA has raised *abort.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code,
+                                          const int* abort = nullptr) {
+  for (long long i = 0; i < kWaitLimit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
+    if (abort && (i & 1023) == 1023 && *(volatile const int*)abort) return false;
+  }
   if (err) atomicCAS(err, 0, code);
   return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
@@ -102,143 +130,340 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
                : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
-  uint32_t r[8];
+// 32 consecutive accumulator columns of this thread's TMEM lane; the caller
+// waits with tmem_wait_ld before reading r.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31}, [%32];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7])
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__global__ void __launch_bounds__(128, 1)
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
     gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA,
                         const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
   extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint8_t* sA = smem;
-  uint8_t* sB = smem + STAGES * A_BYTES;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sB + STAGES * B_BYTES);
-  const uint32_t full0 = smem_u32(bars);             // full[s]  = bars[s]
-  const uint32_t empty0 = smem_u32(bars + STAGES);   // empty[s] = bars[STAGES + s]
-  const uint32_t done = smem_u32(bars + 2 * STAGES);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+  uint8_t* ring = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  float* stage = reinterpret_cast<float*>(ring + RING_BYTES);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(stage + kEpiWarps * 32 * kStageLd);
+  const uint32_t full0 = smem_u32(bars);                       // full[s]
+  const uint32_t empty0 = smem_u32(bars + kMaxStages);         // empty[s]
+  const uint32_t tfull0 = smem_u32(bars + 2 * kMaxStages);     // accumulator a ready
+  const uint32_t tempty0 = smem_u32(bars + 2 * kMaxStages + 2);  // accumulator a drained
+  const uint32_t afull = smem_u32(bars + 2 * kMaxStages + 4);  // resident A block landed
+  const uint32_t afree = smem_u32(bars + 2 * kMaxStages + 5);  // MMAs done with the A block
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kMaxStages + 6);
   __shared__ int s_abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
   const int nk = (g.K + BK - 1) / BK;
+  const int n_tiles = (g.N + BN - 1) / BN;
+  const int m_tiles = (g.M + BM - 1) / BM;
+  const bool resident = g.K <= kResidentK;
+  const int nst = resident ? kStagesResident : kStagesStreamed;
+  // this CTA's contiguous range of output tiles, row-block major
+  const long long total = (long long)m_tiles * n_tiles;
+  const long long t_begin = total * blockIdx.x / gridDim.x;
+  const long long t_end = total * (blockIdx.x + 1) / gridDim.x;
+  // ring addresses: resident A chunks first, then B stages; or A+B per stage
+  auto a_addr = [&](int s, int kt) -> uint8_t* { return resident ? ring + kt * A_BYTES : ring + s * (A_BYTES + B_BYTES); };
+  auto b_addr = [&](int s) -> uint8_t* {
+    return resident ? ring + kResidentChunks * A_BYTES + s * B_BYTES : ring + s * (A_BYTES + B_BYTES) + A_BYTES;
+  };
 
   if (threadIdx.x == 0) {
     s_abort = 0;
-    for (int s = 0; s < STAGES; ++s) {
-      mbar_init(full0 + 8 * s, 1);
-      mbar_init(empty0 + 8 * s, 1);
+    for (int i = 0; i < kMaxStages; ++i) {
+      mbar_init(full0 + 8 * i, 1);
+      mbar_init(empty0 + 8 * i, 1);
     }
-    mbar_init(done, 1);
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(tfull0 + 8 * a, 1);
+      mbar_init(tempty0 + 8 * a, kEpiWarps * 32);
+    }
+    mbar_init(afull, 1);
+    mbar_init(afree, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == kMmaWarp) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(BN));
+                 "r"(2 * BN));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
+  int* abort = &s_abort;
 
-  if (warp == 0 && lane == 0) {
-    // producer: TMA ring
-    int issued = 0;
-    for (int kt = 0; kt < nk; ++kt) {
-      const int s = kt % STAGES, r = kt / STAGES;
-      if (kt >= STAGES && !mbar_wait(empty0 + 8 * s, (r - 1) & 1, g.err, 1)) break;
-      if (*(volatile int*)&s_abort) break;
-      mbar_expect_tx(full0 + 8 * s, A_BYTES + B_BYTES);
-      tma_load_2d(smem_u32(sA + s * A_BYTES), &tmA, kt * BK, m0, full0 + 8 * s);
-      tma_load_2d(smem_u32(sB + s * B_BYTES), &tmB, kt * BK, n0, full0 + 8 * s);
-      issued = kt + 1;
+  if (warp == kProducerWarp) {
+    if (lane == 0) {  // producer: TMA ring
+      int issued = 0, a_loads = 0, cur_mt = -1;
+      bool ok = true;
+      for (long long ti = t_begin; ti < t_end && ok; ++ti) {
+        const int mt = (int)(ti / n_tiles), nt = (int)(ti % n_tiles);
+        if (resident && mt != cur_mt) {
+          // a new row block: wait until the MMAs are done with the old one
+          if (a_loads > 0 && !mbar_wait(afree, (a_loads - 1) & 1, g.err, 6, abort)) {
+            ok = false;
+            break;
+          }
+          mbar_expect_tx(afull, (uint32_t)(nk * A_BYTES));
+          for (int kt = 0; kt < nk; ++kt) tma_load_2d(smem_u32(a_addr(0, kt)), &tmA, kt * BK, mt * BM, afull);
+          ++a_loads;
+          cur_mt = mt;
+        }
+        for (int kt = 0; kt < nk; ++kt) {
+          const int s = issued % nst, r = issued / nst;
+          if (issued >= nst && !mbar_wait(empty0 + 8 * s, (r - 1) & 1, g.err, 1, abort)) {
+            ok = false;
+            break;
+          }
+          if (*(volatile int*)abort) {
+            ok = false;
+            break;
+          }
+          mbar_expect_tx(full0 + 8 * s, resident ? B_BYTES : A_BYTES + B_BYTES);
+          if (!resident) tma_load_2d(smem_u32(a_addr(s, kt)), &tmA, kt * BK, mt * BM, full0 + 8 * s);
+          tma_load_2d(smem_u32(b_addr(s)), &tmB, kt * BK, nt * BN, full0 + 8 * s);
+          ++issued;
+        }
+      }
+      if (!ok) *(volatile int*)abort = 1;
+      // let every copy in flight land before the CTA can exit
+      for (int i = (issued > nst ? issued - nst : 0); i < issued; ++i)
+        mbar_wait(full0 + 8 * (i % nst), (i / nst) & 1, g.err, 2);
+      if (a_loads > 0) mbar_wait(afull, (a_loads - 1) & 1, g.err, 2);
     }
-    // let every copy in flight land before the CTA can exit
-    for (int kt = (issued > STAGES ? issued - STAGES : 0); kt < issued; ++kt)
-      mbar_wait(full0 + 8 * (kt % STAGES), (kt / STAGES) & 1, g.err, 2);
-  } else if (warp == 1 && lane == 0) {
-    // MMA issuer
-    bool ok = true;
-    for (int kt = 0; kt < nk && ok; ++kt) {
-      const int s = kt % STAGES, r = kt / STAGES;
-      if (!mbar_wait(full0 + 8 * s, r & 1, g.err, 3)) {
-        ok = false;
-        *(volatile int*)&s_abort = 1;
+  } else if (warp == kMmaWarp) {
+    if (lane == 0) {  // MMA issuer
+      bool ok = true;
+      int used = 0, t = 0, a_uses = 0, cur_mt = -1;
+      for (long long ti = t_begin; ti < t_end && ok; ++ti, ++t) {
+        const int mt = (int)(ti / n_tiles);
+        if (resident && mt != cur_mt) {
+          if (cur_mt >= 0) mma_commit(afree);  // arrives once the MMAs on the old block finish
+          if (!mbar_wait(afull, a_uses & 1, g.err, 3, abort)) {
+            ok = false;
+            break;
+          }
+          ++a_uses;
+          cur_mt = mt;
+        }
+        const int a = t & 1;
+        if (t >= 2 && !mbar_wait(tempty0 + 8 * a, ((t >> 1) - 1) & 1, g.err, 5, abort)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t d = tmem + (uint32_t)(a * BN);
+        for (int kt = 0; kt < nk; ++kt, ++used) {
+          const int s = used % nst, r = used / nst;
+          if (!mbar_wait(full0 + 8 * s, r & 1, g.err, 3, abort)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint64_t ad = sw128_desc(smem_u32(a_addr(s, kt)));
+          const uint64_t bd = sw128_desc(smem_u32(b_addr(s)));
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; ++kk)  // +32 bytes per K=16 step inside the swizzle atom
+            mma_bf16(d, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), (kt | kk) != 0);
+          mma_commit(empty0 + 8 * s);
+        }
+        if (!ok) break;
+        mma_commit(tfull0 + 8 * a);
+      }
+      if (!ok) *(volatile int*)abort = 1;
+    }
+  } else {
+    // epilogue: warp w owns accumulator rows 32q .. 32q+31 (TMEM lanes,
+    // q = w % 4) and columns 64h .. 64h+63 (h = w / 4); tcgen05.ld is
+    // warp-collective, so the whole warp decides together
+    const int quarter = warp & 3, half = warp >> 2;
+    const int row_l = quarter * 32 + lane;
+    float* wstage = stage + (size_t)warp * 32 * kStageLd;
+    float* srow = wstage + (size_t)lane * kStageLd;
+    // four running maxima (columns i % 4) for instruction-level parallelism;
+    // each keeps its first maximum, and the merge prefers the smaller column
+    // on equal values, so the result is the first maximum of the row
+    float best[4];
+    int best_col[4];
+    auto reset_best = [&]() {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        best[j] = -3.402823466e38f;
+        best_col[j] = -1;
+      }
+    };
+    auto flush_best = [&](int row) {
+      float bb = best[0];
+      int bc = best_col[0];
+#pragma unroll
+      for (int j = 1; j < 4; ++j)
+        if (best_col[j] >= 0 && (bc < 0 || best[j] > bb || (best[j] == bb && best_col[j] < bc))) {
+          bb = best[j];
+          bc = best_col[j];
+        }
+      if (row < g.M && bc >= 0) atomicMax(g.out_argmax + row, argmax_key(bb, bc));
+    };
+    reset_best();
+    const bool has_bias = g.epilogue == kEpiBiasArgmax || g.epilogue == kEpiBiasF32 ||
+                          g.epilogue == kEpiBiasReluBF16;
+    const bool bias_vec = has_bias && ((uintptr_t)g.bias & 15) == 0;
+    const bool vec_ok = g.epilogue != kEpiBiasArgmax && (g.ldc & 3) == 0 &&
+                        ((uintptr_t)g.C & 15) == 0;
+    int t = 0, cur_mt = -1;
+    for (long long ti = t_begin; ti < t_end; ++ti, ++t) {
+      const int mt = (int)(ti / n_tiles), nt = (int)(ti % n_tiles);
+      if (g.epilogue == kEpiBiasArgmax && mt != cur_mt) {
+        if (cur_mt >= 0) flush_best(cur_mt * BM + row_l);
+        reset_best();
+      }
+      cur_mt = mt;
+      const int a = t & 1;
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(tfull0 + 8 * a, (t >> 1) & 1, g.err, 4, abort));
+      if (!ok) {
+        *(volatile int*)abort = 1;
+        cur_mt = -1;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint64_t ad = sw128_desc(smem_u32(sA + s * A_BYTES));
-      const uint64_t bd = sw128_desc(smem_u32(sB + s * B_BYTES));
+      const int m0 = mt * BM, n0 = nt * BN + half * kHalf;
+      const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * BN + half * kHalf);
+      const bool full_cols = n0 + kHalf <= g.N;
+#pragma unroll 1
+      for (int c0 = 0; c0 < kHalf; c0 += kChunk) {
+        uint32_t r[32];
+        tmem_ld32(taddr + (uint32_t)c0, r);
+        // the chunk's bias (same for every row) while the TMEM load is in flight
+        float bv[32];
+        if (has_bias) {
 #pragma unroll
-      for (int kk = 0; kk < BK / 16; ++kk)  // +32 bytes per K=16 step inside the swizzle atom
-        mma_bf16(tmem, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), (kt | kk) != 0);
-      mma_commit(empty0 + 8 * s);
-    }
-    mma_commit(done);
-  }
-  __syncwarp();
-
-  // epilogue: warp w owns accumulator rows 32w .. 32w+31 (TMEM lanes)
-  // tcgen05.ld is warp-collective: the whole warp decides together
-  const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0, g.err, 4) && !*(volatile int*)&s_abort);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const int row = m0 + warp * 32 + lane;
-  float best = -3.402823466e38f;
-  int best_col = 0;
-  if (ok) {
-    for (int c0 = 0; c0 < BN; c0 += 8) {
-      float v[8];
-      tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (row >= g.M) continue;
+          for (int i = 0; i < 32; i += 4) {
+            const int col = n0 + c0 + i;
+            if (bias_vec && col + 3 < g.N) {
+              const float4 b4 = __ldg(reinterpret_cast<const float4*>(g.bias + col));
+              bv[i] = b4.x;
+              bv[i + 1] = b4.y;
+              bv[i + 2] = b4.z;
+              bv[i + 3] = b4.w;
+            } else {
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int col = n0 + c0 + i;
-        if (col >= g.N) continue;
-        float x = v[i];
-        switch (g.epilogue) {
-          case kEpiStoreF32:
-            reinterpret_cast<float*>(g.C)[(size_t)row * g.ldc + col] = x;
-            break;
-          case kEpiAccumF32:
-            reinterpret_cast<float*>(g.C)[(size_t)row * g.ldc + col] += x;
-            break;
-          case kEpiBiasF32:
-            reinterpret_cast<float*>(g.C)[(size_t)row * g.ldc + col] = x + g.bias[col];
-            break;
-          case kEpiBiasReluBF16:
-            x += g.bias[col];
-            reinterpret_cast<__nv_bfloat16*>(g.C)[(size_t)row * g.ldc + col] =
-                __float2bfloat16_rn(x > 0.f ? x : 0.f);
-            break;
-          case kEpiBiasArgmax:
-            x += g.bias[col];
-            if (x > best) {
-              best = x;
-              best_col = col;
+              for (int e = 0; e < 4; ++e) bv[i + e] = col + e < g.N ? __ldg(g.bias + col + e) : 0.f;
             }
-            break;
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) bv[i] = 0.f;
         }
+        tmem_wait_ld();
+        if (c0 + kChunk == kHalf) {  // accumulator drained: hand it back to the MMA issuer
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          mbar_arrive(tempty0 + 8 * a);
+        }
+        if (g.epilogue == kEpiBiasArgmax) {
+          if (full_cols) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              const float x = __uint_as_float(r[i]) + bv[i];
+              if (x > best[i & 3]) {
+                best[i & 3] = x;
+                best_col[i & 3] = n0 + c0 + i;
+              }
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              const int col = n0 + c0 + i;
+              const float x = col < g.N ? __uint_as_float(r[i]) + bv[i] : -3.402823466e38f;
+              if (x > best[i & 3]) {
+                best[i & 3] = x;
+                best_col[i & 3] = col;
+              }
+            }
+          }
+          continue;
+        }
+#pragma unroll
+        for (int i = 0; i < 32; i += 4) {
+          float4 v;
+          v.x = __uint_as_float(r[i]) + bv[i];
+          v.y = __uint_as_float(r[i + 1]) + bv[i + 1];
+          v.z = __uint_as_float(r[i + 2]) + bv[i + 2];
+          v.w = __uint_as_float(r[i + 3]) + bv[i + 3];
+          if (g.epilogue == kEpiBiasReluBF16) {
+            v.x = v.x > 0.f ? v.x : 0.f;
+            v.y = v.y > 0.f ? v.y : 0.f;
+            v.z = v.z > 0.f ? v.z : 0.f;
+            v.w = v.w > 0.f ? v.w : 0.f;
+          }
+          *reinterpret_cast<float4*>(srow + i) = v;
+        }
+        __syncwarp();
+        // the warp's 32 staged rows x 32 columns: 8 lanes per row, 4 rows per pass
+        const int cc = 4 * (lane & 7);
+        const int col = n0 + c0 + cc;
+#pragma unroll
+        for (int pass = 0; pass < 8; ++pass) {
+          const int rr = pass * 4 + (lane >> 3);
+          const int orow = m0 + quarter * 32 + rr;
+          if (orow < g.M) {
+            const float4 v = *reinterpret_cast<const float4*>(wstage + (size_t)rr * kStageLd + cc);
+            if (g.epilogue == kEpiBiasReluBF16) {
+              __nv_bfloat16* c = reinterpret_cast<__nv_bfloat16*>(g.C) + (size_t)orow * g.ldc + col;
+              if (vec_ok && col + 3 < g.N) {
+                __nv_bfloat162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+                uint2 u;
+                u.x = *reinterpret_cast<uint32_t*>(&lo);
+                u.y = *reinterpret_cast<uint32_t*>(&hi);
+                *reinterpret_cast<uint2*>(c) = u;
+              } else {
+                const float vv[4] = {v.x, v.y, v.z, v.w};
+                for (int e = 0; e < 4; ++e)
+                  if (col + e < g.N) c[e] = __float2bfloat16_rn(vv[e]);
+              }
+            } else {
+              float* c = reinterpret_cast<float*>(g.C) + (size_t)orow * g.ldc + col;
+              if (vec_ok && col + 3 < g.N) {
+                float4 o = v;
+                if (g.epilogue == kEpiAccumF32) {
+                  const float4 q = *reinterpret_cast<const float4*>(c);
+                  o.x += q.x;
+                  o.y += q.y;
+                  o.z += q.z;
+                  o.w += q.w;
+                }
+                *reinterpret_cast<float4*>(c) = o;
+              } else {
+                const float vv[4] = {v.x, v.y, v.z, v.w};
+                for (int e = 0; e < 4; ++e)
+                  if (col + e < g.N) c[e] = g.epilogue == kEpiAccumF32 ? c[e] + vv[e] : vv[e];
+              }
+            }
+          }
+        }
+        __syncwarp();
       }
     }
-    if (g.epilogue == kEpiBiasArgmax && row < g.M && best_col < g.N)
-      atomicMax(g.out_argmax + row, argmax_key(best, best_col));
+    if (g.epilogue == kEpiBiasArgmax && cur_mt >= 0) flush_best(cur_mt * BM + row_l);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) {
+  if (warp == kMmaWarp) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
   }
 }
 
@@ -295,8 +520,17 @@ cudaError_t gemm_bf16_tn(const GemmArgs& g, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
-  gemm_bf16_tn_kernel<<<grid, 128, SMEM_BYTES, st>>>(ma, mb, g);
+  // one CTA per SM, each taking a contiguous range of the output tiles
+  static int num_sms = 0;
+  if (num_sms == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      num_sms = 1;
+  }
+  const long long tiles = (long long)((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN);
+  dim3 grid((unsigned)(tiles < num_sms ? tiles : num_sms));
+  gemm_bf16_tn_kernel<<<grid, kThreads, SMEM_BYTES, st>>>(ma, mb, g);
   return cudaGetLastError();
 }
 

@@ -10,7 +10,10 @@ pytestmark = pytest.mark.gpu
 def test_tensor_core_gemm_matches_fp64(lib, cuda):
     import rt_entry_gb300 as r
     rng = np.random.default_rng(0)
-    for M, N, K in [(128, 128, 64), (100, 70, 96), (513, 257, 264), (256, 4096, 256)]:
+    # resident (K <= 256) and streamed A blocks; several column tiles per CTA
+    # (two accumulators in turn) in the last two shapes
+    for M, N, K in [(128, 128, 64), (100, 70, 96), (513, 257, 264), (256, 4096, 256),
+                    (2000, 2048, 320), (10000, 4096, 256)]:
         a = rng.standard_normal((M, K)).astype(np.float32)
         b = rng.standard_normal((N, K)).astype(np.float32)
         ab, bb = r.bf16_bits(a), r.bf16_bits(b)
