@@ -39,7 +39,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "QPS@recall10>=0.95, 1 GB300: learned+BF16 vs plain FP32; HBM GB/s % of peak"
-SWEEP = ((32, 1), (64, 1), (64, 2), (128, 2), (128, 4), (256, 4))
+SWEEP = ((16, 1), (32, 1), (64, 1), (64, 2), (128, 2), (128, 4), (256, 4))
 RECALL_TARGET = 0.95
 LEAF, EXPAND, K_TOP = 32, 0.2, 10
 N_TRAIN = 1_000_000

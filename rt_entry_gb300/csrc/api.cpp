@@ -225,13 +225,13 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   AsyncBuf hits2b;
   if (prm->entry_mode == RTE_ENTRY_KDTREE && !hits) {
     RTE_CUDA(hitsb.alloc((size_t)nq * 4, st));
-    RTE_CUDA(launch_locate(x->d_nodes.p, qp, nq, x->search_dim, hitsb.as<int32_t>(), st));
+    RTE_CUDA(launch_locate(x->d_nodes.p, (int)x->d_nodes.n, qp, nq, x->search_dim, hitsb.as<int32_t>(), st));
     hits = hitsb.as<int32_t>();
   }
   if (prm->entry_mode == RTE_ENTRY_LEARNED) {
     // proposed leaf (MLP) first, kd-tree leaf second
     RTE_CUDA(hits2b.alloc((size_t)nq * 4, st));
-    RTE_CUDA(launch_locate(x->d_nodes.p, qp, nq, x->search_dim, hits2b.as<int32_t>(), st));
+    RTE_CUDA(launch_locate(x->d_nodes.p, (int)x->d_nodes.n, qp, nq, x->search_dim, hits2b.as<int32_t>(), st));
     hits2 = hits2b.as<int32_t>();
     if (!hits) {
       RTE_CUDA(hitsb.alloc((size_t)nq * 4, st));
@@ -485,7 +485,7 @@ rte_status rte_locate(rte_index* x, const float* projected, int64_t nq, int32_t*
     RTE_CUDA(ob.alloc((size_t)nq * 4, st));
     dout = ob.as<int32_t>();
   }
-  RTE_CUDA(launch_locate(x->d_nodes.p, dp, nq, x->search_dim, dout, st));
+  RTE_CUDA(launch_locate(x->d_nodes.p, (int)x->d_nodes.n, dp, nq, x->search_dim, dout, st));
   if (!od) {
     RTE_CUDA(cudaMemcpyAsync(out_leaf, dout, (size_t)nq * 4, cudaMemcpyDeviceToHost, st));
     RTE_CUDA(cudaStreamSynchronize(st));

@@ -161,6 +161,31 @@ bool kd_build(const float* xyz, int64_t n, int cap, KdTree& out, std::string& er
     stack.push_back({mid, f.r, right, f.depth + 1});
     stack.push_back({f.l, mid, left, f.depth + 1});
   }
+  // renumber the nodes breadth-first (structure and leaf ids unchanged), so
+  // that the top levels of the tree are the first nodes of the array
+  {
+    std::vector<int> order;
+    order.reserve(out.nodes.size());
+    order.push_back(0);
+    for (size_t h = 0; h < order.size(); ++h) {
+      const BvhNode& nd = out.nodes[order[h]];
+      if (nd.left >= 0) {
+        order.push_back(nd.left);
+        order.push_back(nd.right);
+      }
+    }
+    std::vector<int> renum(out.nodes.size());
+    for (size_t i = 0; i < order.size(); ++i) renum[order[i]] = (int)i;
+    std::vector<BvhNode> bfs(order.size());
+    for (size_t i = 0; i < order.size(); ++i) {
+      bfs[i] = out.nodes[order[i]];
+      if (bfs[i].left >= 0) {
+        bfs[i].left = renum[bfs[i].left];
+        bfs[i].right = renum[bfs[i].right];
+      }
+    }
+    out.nodes.swap(bfs);
+  }
   const int64_t nl = out.n_leaves;
   out.pids.assign(nl * cap, (int32_t)n);
   std::vector<int32_t> fill(nl, 0);
@@ -183,6 +208,7 @@ void kd_expand(KdTree& t, float ratio) {
     }
   }
   // bounds bottom-up: children always have larger node indices than parents
+  // (breadth-first numbering)
   for (int64_t k = (int64_t)t.nodes.size() - 1; k >= 0; --k) {
     BvhNode& nd = t.nodes[k];
     if (nd.left < 0) {

@@ -106,37 +106,44 @@ __global__ void cov_finish(const double* __restrict__ partial, int nchunks, int 
 }
 
 // ---------------------------------------------------------- projection ----
-// out[r][j] = sum_c (x[r][c] - mean[c]) * V[c][j] for j < k, FP32 FMA chain
-// in c order.  64 rows x 32 columns per block; x and V staged in shared
-// memory in 32-wide slices of c.
-constexpr int kPrRows = 64;
-constexpr int kPrCols = 32;
+// out[r][j] = sum_c (x[r][c] - mean[c]) * V[c][j], one fmaf per c in
+// ascending order.  A block computes a 32 x 128 tile; each thread an 8 x 4
+// register tile, so every shared-memory read feeds 4 (x) or 8 (V) FMAs.
+constexpr int kPrRows = 32;
+constexpr int kPrCols = 128;
 constexpr int kPrK = 32;
 
-__global__ void project_rows(const float* __restrict__ x, int64_t n, int d, int xstride,
-                             const float* __restrict__ mean, const float* __restrict__ V, int vstride,
-                             int k, float* __restrict__ out, int ostride,
-                             const int* __restrict__ n_dev) {
+__global__ void __launch_bounds__(128) project_rows(const float* __restrict__ x, int64_t n, int d,
+                                                    int xstride, const float* __restrict__ mean,
+                                                    const float* __restrict__ V, int vstride, int k,
+                                                    float* __restrict__ out, int ostride,
+                                                    const int* __restrict__ n_dev) {
   if (n_dev) n = min(n, (int64_t)*n_dev);  // graph replay: rows beyond the batch are idle
   if ((int64_t)blockIdx.x * kPrRows >= n) return;
   __shared__ float sx[kPrRows][kPrK + 1];
-  __shared__ float sv[kPrK][kPrCols];
+  __shared__ __align__(16) float sv[kPrK][kPrCols];
   const int64_t row0 = (int64_t)blockIdx.x * kPrRows;
   const int col0 = blockIdx.y * kPrCols;
-  const int tx = threadIdx.x & 31;   // column
-  const int ty = threadIdx.x >> 5;   // 8 row groups
-  float acc[kPrRows / 8];
+  const int tx = threadIdx.x & 31;  // columns 4tx .. 4tx+3
+  const int ty = threadIdx.x >> 5;  // rows 8ty .. 8ty+7
+  float acc[8][4];
 #pragma unroll
-  for (int i = 0; i < kPrRows / 8; ++i) acc[i] = 0.0f;
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
   for (int c0 = 0; c0 < d; c0 += kPrK) {
-    for (int t = threadIdx.x; t < kPrRows * kPrK; t += blockDim.x) {
+#pragma unroll
+    for (int u = 0; u < kPrRows * kPrK / 128; ++u) {
+      const int t = threadIdx.x + 128 * u;
       const int rr = t / kPrK, cc = t % kPrK;
       const int64_t r = row0 + rr;
       float v = 0.0f;
       if (r < n && c0 + cc < d) v = __fsub_rn(x[r * xstride + c0 + cc], mean ? mean[c0 + cc] : 0.0f);
       sx[rr][cc] = v;
     }
-    for (int t = threadIdx.x; t < kPrK * kPrCols; t += blockDim.x) {
+#pragma unroll 4
+    for (int u = 0; u < kPrK * kPrCols / 128; ++u) {
+      const int t = threadIdx.x + 128 * u;
       const int cc = t / kPrCols, jj = t % kPrCols;
       float v = 0.0f;
       if (c0 + cc < d && col0 + jj < k) v = V[(int64_t)(c0 + cc) * vstride + col0 + jj];
@@ -145,19 +152,28 @@ __global__ void project_rows(const float* __restrict__ x, int64_t n, int d, int 
     __syncthreads();
 #pragma unroll 8
     for (int cc = 0; cc < kPrK; ++cc) {
-      const float vv = sv[cc][tx];
+      const float4 v = *reinterpret_cast<const float4*>(&sv[cc][4 * tx]);
 #pragma unroll
-      for (int i = 0; i < kPrRows / 8; ++i) acc[i] = __fmaf_rn(sx[ty + 8 * i][cc], vv, acc[i]);
+      for (int i = 0; i < 8; ++i) {
+        const float xv = sx[8 * ty + i][cc];
+        acc[i][0] = __fmaf_rn(xv, v.x, acc[i][0]);
+        acc[i][1] = __fmaf_rn(xv, v.y, acc[i][1]);
+        acc[i][2] = __fmaf_rn(xv, v.z, acc[i][2]);
+        acc[i][3] = __fmaf_rn(xv, v.w, acc[i][3]);
+      }
     }
     __syncthreads();
   }
-  const int j = col0 + tx;
-  if (j < k)
 #pragma unroll
-    for (int i = 0; i < kPrRows / 8; ++i) {
-      const int64_t r = row0 + ty + 8 * i;
-      if (r < n) out[r * ostride + j] = acc[i];
+  for (int i = 0; i < 8; ++i) {
+    const int64_t r = row0 + 8 * ty + i;
+    if (r >= n) break;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int col = col0 + 4 * tx + j;
+      if (col < k) out[r * ostride + col] = acc[i][j];
     }
+  }
 }
 
 // ---------------------------------------------------------- interleave ----
@@ -236,11 +252,29 @@ __global__ void dequant_rows(const void* __restrict__ il, const float* __restric
 // the union of its leaves' expanded boxes.  Leaves are numbered in the same
 // order, so the first leaf whose box contains the point is the smallest such
 // index (canonical rule for the ray cast's arbitrary hit).
-__global__ void locate_points(const BvhNode* __restrict__ nodes, const float* __restrict__ pts,
-                              int64_t n, int stride, int32_t* __restrict__ out,
-                              const int* __restrict__ n_dev) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// The first kTopNodes nodes (breadth-first numbering: the top ten levels)
+// are copied into shared memory by every block; deeper nodes are read from
+// global memory.
+constexpr int kTopNodes = 1023;
+
+__device__ __forceinline__ void load_top_nodes(const BvhNode* __restrict__ nodes, int n_nodes,
+                                               BvhNode* top) {
+  const int ntop = min(kTopNodes, n_nodes);
+  const float4* src = reinterpret_cast<const float4*>(nodes);
+  float4* dst = reinterpret_cast<float4*>(top);
+  for (int i = threadIdx.x; i < 2 * ntop; i += blockDim.x) dst[i] = __ldg(src + i);
+  __syncthreads();
+}
+
+__global__ void locate_points(const BvhNode* __restrict__ nodes, int n_nodes,
+                              const float* __restrict__ pts, int64_t n, int stride,
+                              int32_t* __restrict__ out, const int* __restrict__ n_dev) {
+  __shared__ BvhNode top[kTopNodes];
   if (n_dev) n = min(n, (int64_t)*n_dev);
+  if ((int64_t)blockIdx.x * blockDim.x >= n) return;
+  load_top_nodes(nodes, n_nodes, top);
+  const int ntop = min(kTopNodes, n_nodes);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float x = pts[i * stride + 0], y = pts[i * stride + 1], z = pts[i * stride + 2];
   int stack[kBvhMaxDepth];
@@ -248,7 +282,8 @@ __global__ void locate_points(const BvhNode* __restrict__ nodes, const float* __
   stack[sp++] = 0;
   int32_t hit = 0;
   while (sp > 0) {
-    const BvhNode nd = nodes[stack[--sp]];
+    const int k = stack[--sp];
+    const BvhNode nd = k < ntop ? top[k] : nodes[k];
     if (!(nd.lo[0] <= x && x <= nd.hi[0] && nd.lo[1] <= y && y <= nd.hi[1] && nd.lo[2] <= z &&
           z <= nd.hi[2]))
       continue;
@@ -329,7 +364,7 @@ cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const 
                            cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  project_rows<<<grid, 256, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr);
+  project_rows<<<grid, 128, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr);
   return cudaGetLastError();
 }
 
@@ -337,7 +372,7 @@ cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, in
                                const float* mean, const float* V, int vstride, int k, float* out,
                                int ostride, cudaStream_t st) {
   dim3 grid((unsigned)((cap + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  project_rows<<<grid, 256, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride, n_dev);
+  project_rows<<<grid, 128, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride, n_dev);
   return cudaGetLastError();
 }
 
@@ -365,16 +400,18 @@ cudaError_t launch_dequant(const void* il, const float* scale8, int precision, i
   return cudaGetLastError();
 }
 
-cudaError_t launch_locate(const BvhNode* nodes, const float* pts, int64_t n, int stride,
+// 64 points per block: enough blocks to spread a batch of a few thousand
+// points over every SM (each block copies the top of the tree once).
+cudaError_t launch_locate(const BvhNode* nodes, int n_nodes, const float* pts, int64_t n, int stride,
                           int32_t* out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  locate_points<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(nodes, pts, n, stride, out, nullptr);
+  locate_points<<<(unsigned)((n + 63) / 64), 64, 0, st>>>(nodes, n_nodes, pts, n, stride, out, nullptr);
   return cudaGetLastError();
 }
 
-cudaError_t launch_locate_dyn(const BvhNode* nodes, const float* pts, int64_t cap, const int* n_dev,
-                              int stride, int32_t* out, cudaStream_t st) {
-  locate_points<<<(unsigned)((cap + 127) / 128), 128, 0, st>>>(nodes, pts, cap, stride, out, n_dev);
+cudaError_t launch_locate_dyn(const BvhNode* nodes, int n_nodes, const float* pts, int64_t cap,
+                              const int* n_dev, int stride, int32_t* out, cudaStream_t st) {
+  locate_points<<<(unsigned)((cap + 63) / 64), 64, 0, st>>>(nodes, n_nodes, pts, cap, stride, out, n_dev);
   return cudaGetLastError();
 }
 

@@ -31,8 +31,8 @@ cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const 
 cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, int d, int xstride,
                                const float* mean, const float* V, int vstride, int k, float* out,
                                int ostride, cudaStream_t st);
-cudaError_t launch_locate_dyn(const BvhNode* nodes, const float* pts, int64_t cap, const int* n_dev,
-                              int stride, int32_t* out, cudaStream_t st);
+cudaError_t launch_locate_dyn(const BvhNode* nodes, int n_nodes, const float* pts, int64_t cap,
+                              const int* n_dev, int stride, int32_t* out, cudaStream_t st);
 cudaError_t launch_interleave(const float* src, int64_t n, int d, int C, float* il32, void* il16,
                               uint8_t* il8, float* scale8, float* xyz, cudaStream_t st);
 cudaError_t launch_deinterleave(const float* il32, int64_t n, int d, int C, float* dst,
@@ -42,7 +42,7 @@ cudaError_t launch_dequant(const void* il, const float* scale8, int precision, i
 cudaError_t launch_locate_in_subtree(const BvhNode* nodes, const float* pts, int64_t n, int stride,
                                      const int32_t* cls, const int32_t* start_node,
                                      const int32_t* fallback_leaf, int32_t* out, cudaStream_t st);
-cudaError_t launch_locate(const BvhNode* nodes, const float* pts, int64_t n, int stride,
+cudaError_t launch_locate(const BvhNode* nodes, int n_nodes, const float* pts, int64_t n, int stride,
                           int32_t* out, cudaStream_t st);
 
 }  // namespace rte
