@@ -53,7 +53,7 @@ namespace {
 
 size_t index_bytes(const rte_index* x) {
   return x->raw.bytes() + x->graph.bytes() + x->d_mean.bytes() + x->d_rot.bytes() +
-         x->il32.bytes() + x->il16.bytes() + x->il8.bytes() + x->scale8.bytes() +
+         x->il32.bytes() + x->il16.bytes() + x->il8.bytes() + x->scale8.bytes() + x->norm16.bytes() +
          x->d_nodes.bytes() + x->d_pids.bytes();
 }
 
@@ -66,11 +66,13 @@ rte_status make_search_space(rte_index* x, const float* rm) {
   RTE_CUDA(x->il16.alloc(row * x->np));
   RTE_CUDA(x->il8.alloc(row * x->np));
   RTE_CUDA(x->scale8.alloc(x->np));
+  RTE_CUDA(x->norm16.alloc(x->np));
   DevBuf<float> xyz;
   RTE_CUDA(xyz.alloc(3 * x->np));
   if (x->search_dim < 3) RTE_CUDA(cudaMemset(xyz.p, 0, xyz.bytes()));
   RTE_CUDA(launch_interleave(rm, x->np, x->search_dim, x->C, x->il32.p, x->il16.p, x->il8.p,
                              x->scale8.p, xyz.p, 0));
+  RTE_CUDA(launch_bf16_norms(x->il16.p, x->np, x->C, x->norm16.p, 0));
   x->xyz.resize(3 * x->np);
   RTE_CUDA(cudaMemcpy(x->xyz.data(), xyz.p, xyz.bytes(), cudaMemcpyDeviceToHost));
   RTE_CUDA(cudaDeviceSynchronize());
@@ -184,7 +186,7 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
   pl.prec = prm->precision;
   // per warp: the bloom filter plus the compaction buffers (ids, distances)
   const int S = std::max(B, pl.L);
-  const size_t per_warp = (size_t)(prm->bloom_words + 2 * S) * 4;
+  const size_t per_warp = (size_t)(prm->bloom_words + 2 * S + kQuerySlotWords) * 4;
   const size_t smem_cap = 227 * 1024;
   if (prm->warps_per_block > 0) {
     pl.wpb = prm->warps_per_block;
@@ -247,6 +249,7 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   a.base_bf16 = x->il16.p;
   a.base_fp8 = x->il8.p;
   a.fp8_scale = x->scale8.p;
+  a.norm16 = x->norm16.p;
   a.queries = qp;
   a.graph = x->graph.p;
   a.leaf_pids = x->has_kdtree ? x->d_pids.p : nullptr;

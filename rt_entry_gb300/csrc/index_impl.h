@@ -131,6 +131,7 @@ struct rte_index {
   rte::DevBuf<uint16_t> il16;
   rte::DevBuf<uint8_t> il8;
   rte::DevBuf<float> scale8;
+  rte::DevBuf<float> norm16;  // squared norms of the BF16 rows
   std::vector<float> xyz;  // first three search-space coordinates [np][3]
   // kd-tree
   bool has_kdtree = false;

@@ -331,6 +331,25 @@ __global__ void locate_in_subtree(const BvhNode* __restrict__ nodes, const float
   out[i] = hit;
 }
 
+// One warp per row: the squared norm of the BF16 row, summed in FP64 in a
+// fixed order (lane partials, then a butterfly), rounded to FP32.
+__global__ void bf16_norms(const uint16_t* __restrict__ il16, int64_t n, int C,
+                           float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n; r += nwarps) {
+    const uint16_t* row = il16 + r * 32 * C;
+    double s = 0.0;
+    for (int e = lane; e < 32 * C; e += 32) {
+      const double v = (double)__uint_as_float((uint32_t)row[e] << 16);
+      s += v * v;
+    }
+    for (int off = 16; off >= 1; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) out[r] = (float)s;
+  }
+}
+
 // -------------------------------------------------------------- launches ----
 cudaError_t launch_locate_in_subtree(const BvhNode* nodes, const float* pts, int64_t n, int stride,
                                      const int32_t* cls, const int32_t* start_node,
@@ -390,6 +409,13 @@ cudaError_t launch_deinterleave(const float* il32, int64_t n, int d, int C, floa
                                 cudaStream_t st) {
   const int64_t blocks = std::min<int64_t>((n + 7) / 8, 65535 * 8);
   deinterleave_rows<<<(unsigned)blocks, 256, 0, st>>>(il32, n, d, C, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bf16_norms(const uint16_t* il16, int64_t n, int C, float* out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((n + 7) / 8, 4096);
+  bf16_norms<<<(unsigned)blocks, 256, 0, st>>>(il16, n, C, out);
   return cudaGetLastError();
 }
 

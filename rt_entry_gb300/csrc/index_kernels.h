@@ -37,6 +37,9 @@ cudaError_t launch_interleave(const float* src, int64_t n, int d, int C, float* 
                               uint8_t* il8, float* scale8, float* xyz, cudaStream_t st);
 cudaError_t launch_deinterleave(const float* il32, int64_t n, int d, int C, float* dst,
                                 cudaStream_t st);
+// Squared norm of every BF16 row (FP64 sum of the BF16 values squared,
+// rounded to FP32).
+cudaError_t launch_bf16_norms(const uint16_t* il16, int64_t n, int C, float* out, cudaStream_t st);
 cudaError_t launch_dequant(const void* il, const float* scale8, int precision, int64_t n, int d,
                            int C, float* dst, cudaStream_t st);
 cudaError_t launch_locate_in_subtree(const BvhNode* nodes, const float* pts, int64_t n, int stride,

@@ -105,6 +105,7 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   a.base_bf16 = x->il16.p;
   a.base_fp8 = x->il8.p;
   a.fp8_scale = x->scale8.p;
+  a.norm16 = x->norm16.p;
   a.queries = projected;
   a.graph = x->graph.p;
   a.leaf_pids = x->has_kdtree ? x->d_pids.p : nullptr;

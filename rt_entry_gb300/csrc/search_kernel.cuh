@@ -250,6 +250,108 @@ __device__ __forceinline__ float lane_partial(const float (&p)[C], const float (
   return s;
 }
 
+// ---- BF16 distances on the tensor cores (rows of 32*C <= 128 dims) ----
+// dist = |p|^2 + |q|^2 - 2 p.q, p the BF16 row, q the query rounded to BF16,
+// p.q from mma.sync m16n8k16 (BF16 inputs, exact products, FP32
+// accumulation).  A BF16 row (32*C values, 64*C bytes) is read as C pieces
+// of 64 bytes; thread t of each 4-thread group reads bytes [16t + 64i, +16)
+// of piece i -- storage elements 32i + 8t + j, j < 8 -- and uses them as the
+// MMA k-slots {2t, 2t+1, 2t+8, 2t+9} of k-tiles 2i (j < 4) and 2i+1 (j >= 4).
+// The query fragment comes from the query's own BF16 row at the same storage
+// positions, so each k pairs the base and query values of one dimension.
+// With integer-valued data of magnitude < 2^8 every term is exact and the
+// distances equal the FP32 path's bit for bit.
+template <int C, int PREC, bool MMA = (PREC == kPrecBF16 && C <= 4)>
+struct QueryExtra {};
+template <int C, int PREC>
+struct QueryExtra<C, PREC, true> {
+  const uint32_t* qs;  // the query's BF16 row in the warp's shared memory (16*C words)
+  float qn;            // squared norm of the BF16 query
+};
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2,
+                                               uint32_t a3, uint32_t b0, uint32_t b1) {
+  asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+      "{%8, %9}, {%0, %1, %2, %3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// The query in the base's BF16 layout, kept in `slot` (16*C words of the
+// warp's shared memory) for the whole query, and its squared norm.
+template <int C>
+__device__ __forceinline__ void make_query_extra(QueryExtra<C, kPrecBF16, true>& qx,
+                                                 const float (&qv)[C], uint32_t* slot, int lane) {
+  uint16_t* qs = reinterpret_cast<uint16_t*>(slot);
+  float s = 0.0f;
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const __nv_bfloat16 b = __float2bfloat16_rn(qv[c]);
+    const float f = __bfloat162float(b);
+    s = __fmaf_rn(f, f, s);
+    qs[interleaved_offset(c, lane, C)] = __bfloat16_as_ushort(b);
+  }
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) s = __fadd_rn(s, __shfl_xor_sync(kFull, s, off));
+  qx.qn = s;
+  qx.qs = slot;
+  __syncwarp();
+}
+
+// Requests every valid row's 128-byte lines into L2 (lines spread over the
+// lanes), so the gathers below find their rows in flight or in L2.
+template <int kRowBytes>
+__device__ __forceinline__ void prefetch_rows(const char* rows, const int* s_ids, int n, int lane) {
+  constexpr int kLines = (kRowBytes + 127) / 128;
+  for (int i = lane; i < n * kLines; i += 32) {
+    const int row = i / kLines, line = i - row * kLines;
+    const char* p = rows + (size_t)s_ids[row] * kRowBytes + line * 128;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+  }
+}
+
+// Distances of the n ids in s_ids[0..n) by the tensor cores, 8 rows per MMA
+// group: thread (g, t) supplies row g of the group as column g of the MMA's
+// B operand; the query is every row of A, so D[.][col] is the dot product of
+// row col, and lanes 0..3 hold the group's eight results.
+template <int C>
+__device__ __forceinline__ void distances_mma(const SearchArgs& a, const QueryExtra<C, kPrecBF16, true>& qx,
+                                              const int* s_ids, float* s_dist, int n, int lane) {
+  constexpr int kRowBytes = 64 * C;
+  const char* rows = reinterpret_cast<const char*>(a.base_bf16);
+  prefetch_rows<kRowBytes>(rows, s_ids, n, lane);
+  const int g = lane >> 2, t = lane & 3;
+  for (int r0 = 0; r0 < n; r0 += 8) {
+    const int ra = r0 + g;
+    const int id = s_ids[ra < n ? ra : r0];
+    const char* p = rows + (size_t)id * kRowBytes + 16 * t;
+    uint4 v[C];
+#pragma unroll
+    for (int i = 0; i < C; ++i) v[i] = __ldg(reinterpret_cast<const uint4*>(p + 64 * i));
+    // the norms of this lane's two output rows, loaded while the MMAs run
+    float pn[2] = {0.0f, 0.0f};
+    if (g == 0) {
+#pragma unroll
+      for (int e = 0; e < 2; ++e)
+        if (r0 + 2 * t + e < n) pn[e] = __ldg(a.norm16 + s_ids[r0 + 2 * t + e]);
+    }
+    float d[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int i = 0; i < C; ++i) {
+      const uint4 q = *reinterpret_cast<const uint4*>(qx.qs + 4 * t + 16 * i);
+      mma_bf16_16816(d, q.x, q.x, q.y, q.y, v[i].x, v[i].y);
+      mma_bf16_16816(d, q.z, q.z, q.w, q.w, v[i].z, v[i].w);
+    }
+    if (g == 0) {
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int row = r0 + 2 * t + e;
+        if (row < n) s_dist[row] = __fmaf_rn(-2.0f, d[e], __fadd_rn(pn[e], qx.qn));
+      }
+    }
+  }
+}
+
 // Distances of the n (<= B) ids in s_ids[0..n) written to s_dist[0..n).
 // Groups of G rows (16, or 8 for long rows): each lane forms its partial for
 // the G rows; a butterfly over offsets 16, 8, ... exchanges half of the rows
@@ -259,23 +361,20 @@ __device__ __forceinline__ float lane_partial(const float (&p)[C], const float (
 // shuffle-down tree (addition is commutative, so the results are equal).
 template <int C, int PREC>
 __device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)[C],
-                                          const int* s_ids, float* s_dist, int n, int lane) {
+                                          const QueryExtra<C, PREC>& qx, const int* s_ids,
+                                          float* s_dist, int n, int lane) {
+  if constexpr (PREC == kPrecBF16 && C <= 4) {
+    distances_mma<C>(a, qx, s_ids, s_dist, n, lane);
+    return;
+  }
   constexpr int G = C <= 4 ? 8 : 2;
   constexpr int SPAN = 32 / G;  // lanes sharing one row after the butterfly
-  // Every valid row is requested into L2 up front (128-byte lines spread
-  // over the lanes), so the groups below find their rows in flight or in L2
-  // instead of paying one memory latency each.
   {
     constexpr int kRowBytes = 32 * C * (PREC == kPrecF32 ? 4 : PREC == kPrecBF16 ? 2 : 1);
-    constexpr int kLines = (kRowBytes + 127) / 128;
     const char* rows = PREC == kPrecF32    ? reinterpret_cast<const char*>(a.base)
                        : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
                                            : reinterpret_cast<const char*>(a.base_fp8);
-    for (int i = lane; i < n * kLines; i += 32) {
-      const int row = i / kLines, line = i - row * kLines;
-      const char* p = rows + (size_t)s_ids[row] * kRowBytes + line * 128;
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-    }
+    prefetch_rows<kRowBytes>(rows, s_ids, n, lane);
   }
   for (int g0 = 0; g0 < n; g0 += G) {
     // all G loads first, unconditionally (a short group re-reads its first
@@ -308,8 +407,9 @@ __device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)
 // compute their distances, and scatter them back (invalid slots -> MAX).
 template <int C, int NB, int PREC>
 __device__ __forceinline__ int batch_distances(const SearchArgs& a, const float (&qv)[C],
-                                               float (&bd)[NB], const int (&bi)[NB], int* s_ids,
-                                               float* s_dist, int lane) {
+                                               const QueryExtra<C, PREC>& qx, float (&bd)[NB],
+                                               const int (&bi)[NB], int* s_ids, float* s_dist,
+                                               int lane) {
   const unsigned lt = (1u << lane) - 1u;
   int kidx[NB];
   int n = 0;
@@ -322,7 +422,7 @@ __device__ __forceinline__ int batch_distances(const SearchArgs& a, const float 
     n += __popc(m);
   }
   __syncwarp();
-  distances<C, PREC>(a, qv, s_ids, s_dist, n, lane);
+  distances<C, PREC>(a, qv, qx, s_ids, s_dist, n, lane);
   __syncwarp();
 #pragma unroll
   for (int j = 0; j < NB; ++j) bd[j] = kidx[j] >= 0 ? s_dist[kidx[j]] : kMaxDist;
@@ -354,7 +454,7 @@ __device__ __forceinline__ void rerank_pool(const SearchArgs& a, const float (&q
     n += __popc(m);
   }
   __syncwarp();
-  distances<C, kPrecF32>(a, qv, s_ids, s_dist, n, lane);
+  distances<C, kPrecF32>(a, qv, QueryExtra<C, kPrecF32>{}, s_ids, s_dist, n, lane);
   __syncwarp();
 #pragma unroll
   for (int j = 0; j < PR; ++j) pd[j] = kidx[j] >= 0 ? s_dist[kidx[j]] : kMaxDist;
@@ -364,14 +464,14 @@ __device__ __forceinline__ void rerank_pool(const SearchArgs& a, const float (&q
 
 template <int C, int NL, int NB, int PREC>
 __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& bloom, int* s_ids,
-                             float* s_dist) {
+                             float* s_dist, uint32_t* q_slot) {
   constexpr int L = pool_slots(NL);
   constexpr int PR = pool_regs(NL);  // pool registers
   constexpr int B = 32 * NB;
   const int np = a.np;
   const int R = a.R;
   const int NR = R >> 5;  // batch registers per expanded node
-  long long c_entries = 0, c_expanded = 0, c_dists = 0;
+  int c_entries = 0, c_expanded = 0, c_dists = 0;  // per query: far below 2^31
 
   float qv[C];
 #pragma unroll
@@ -389,6 +489,9 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
   }
   float bd[NB];
   int bi[NB];
+
+  QueryExtra<C, PREC> qx;
+  if constexpr (PREC == kPrecBF16 && C <= 4) make_query_extra<C>(qx, qv, q_slot, lane);
 
   bloom.clear(lane);
   __syncwarp();
@@ -430,7 +533,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
       bi[j] = id;
     }
     __syncwarp();
-    c_entries += batch_distances<C, NB, PREC>(a, qv, bd, bi, s_ids, s_dist, lane);
+    c_entries += batch_distances<C, NB, PREC>(a, qv, qx, bd, bi, s_ids, s_dist, lane);
     sort_batch_desc<NB>(bd, bi, lane);
     merge_pool<NL, NB>(pd, pi, bd, bi, false, lane);
   }
@@ -524,7 +627,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
       __syncwarp();
     }
 
-    c_dists += batch_distances<C, NB, PREC>(a, qv, bd, bi, s_ids, s_dist, lane);
+    c_dists += batch_distances<C, NB, PREC>(a, qv, qx, bd, bi, s_ids, s_dist, lane);
     sort_batch_desc<NB>(bd, bi, lane);
     merge_pool<NL, NB>(pd, pi, bd, bi, true, lane);
 
@@ -581,7 +684,7 @@ __global__ void __launch_bounds__(256, (C <= 4 ? 4 : 2)) search_kernel(SearchArg
   const int wib = threadIdx.x >> 5;
   constexpr int B = 32 * NB;
   constexpr int S = B > pool_slots(NL) ? B : pool_slots(NL);  // compaction slots per warp
-  const int per_warp = a.bloom_words + 2 * S;
+  const int per_warp = a.bloom_words + 2 * S + kQuerySlotWords;
   uint32_t* wbase = smem + (size_t)wib * per_warp;
   Bloom bloom;
   bloom.w = wbase;
@@ -597,7 +700,8 @@ __global__ void __launch_bounds__(256, (C <= 4 ? 4 : 2)) search_kernel(SearchArg
     if (lane == 0) q = (int)atomicAdd(a.work, 1u);
     q = __shfl_sync(kFull, q, 0);
     if (q >= nq) break;
-    search_query<C, NL, NB, PREC>(a, q, lane, bloom, s_ids, s_dist);
+    search_query<C, NL, NB, PREC>(a, q, lane, bloom, s_ids, s_dist,
+                                  reinterpret_cast<uint32_t*>(s_dist + S));
   }
 }
 

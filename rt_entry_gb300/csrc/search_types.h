@@ -6,11 +6,17 @@ namespace rte {
 
 enum : int { kPrecF32 = 0, kPrecBF16 = 1, kPrecFP8 = 2 };
 
+// Shared memory of one warp of the search kernel, in 32-bit words: the bloom
+// filter, 2*max(batch, beam) compaction slots, and a slot for the query's
+// BF16 row (tensor-core distances, up to 128 dims).
+constexpr int kQuerySlotWords = 64;
+
 struct SearchArgs {
   const float* base;        // lane-interleaved FP32 rows, stride 32*C floats
   const uint16_t* base_bf16;  // lane-interleaved BF16 rows (precision 1)
   const uint8_t* base_fp8;  // lane-interleaved E4M3 rows (precision 2)
   const float* fp8_scale;   // per-row scale (precision 2)
+  const float* norm16;      // per-row squared norm of the BF16 row (precision 1, d <= 128)
   const float* queries;     // row-major [nq][qstride]
   const int32_t* graph;     // [np][R], padding np
   const int32_t* leaf_pids; // [n_leaves][leaf_cap], padding np

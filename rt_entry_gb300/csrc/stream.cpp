@@ -78,6 +78,7 @@ rte_status capture(rte_batcher* b) {
     a.base_bf16 = x->il16.p;
     a.base_fp8 = x->il8.p;
     a.fp8_scale = x->scale8.p;
+    a.norm16 = x->norm16.p;
     a.queries = qp;
     a.graph = x->graph.p;
     a.leaf_pids = x->has_kdtree ? x->d_pids.p : nullptr;

@@ -192,8 +192,11 @@ def test_locate_matches_oracle_including_faces(lib, orc, cuda):
 @pytest.mark.parametrize("prec", [1, 2])
 @pytest.mark.parametrize("rerank", [0, 1])
 def test_low_precision_paths_match_oracle(lib, orc, cuda, prec, rerank, L):
+    """BF16 (d <= 128) forms its dot products on the tensor cores, which is
+    bit-exact with the oracle when every term is exact: integer-valued data.
+    FP8 runs the oracle's own operations, on any data."""
     from rt_entry_gb300 import datasets as ds
-    base, q = _mixture(3000, 200, 128, False, seed=31 + prec)
+    base, q = _mixture(3000, 200, 128, prec == 1, seed=31 + prec)
     graph = ds.knn_graph(base, 64)
     idx = _index(base, graph, 32, 0.2)
     _, _, pids = idx.kdtree()
@@ -211,6 +214,42 @@ def test_low_precision_paths_match_oracle(lib, orc, cuda, prec, rerank, L):
                           rerank_base=base if rerank else None)
     assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
     assert np.array_equal(dd, od)
+
+
+@pytest.mark.parametrize("d", [128, 96])
+def test_bf16_tensor_core_distances_on_real_valued_data(lib, orc, cuda, d):
+    """Real-valued data: the BF16 distance is |p|^2 + |q|^2 - 2 p.q with the
+    query rounded to BF16 and FP32 sums, so it differs from the oracle's
+    sum of (p - q)^2 by roundings.  Bars: every returned distance within
+    1e-5 of the squared-norm scale of the same formula in FP64; top-10
+    agreement with the oracle >= 0.98; after the FP32 rerank, distances of
+    the returned ids within FP32 rounding of FP64 and sorted; recall within
+    0.01 of the FP32 search."""
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(3000, 200, d, False, seed=77 + d)
+    graph = ds.knn_graph(base, 64)
+    idx = _index(base, graph, 32, 0.2)
+    _, _, pids = idx.kdtree()
+    hits = idx.locate(q)
+    low = idx.search_base_lowp(1).astype(np.float64)
+    qb = (r.bf16_bits(q).astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    ids, dd = idx.search_projected(q, beam=64, k=64, precision=1, rerank=0)
+    ref = ((low[ids] - qb[:, None, :]) ** 2).sum(-1)
+    scale = (low ** 2).sum(1).max() + (qb ** 2).sum(1).max()
+    assert np.abs(dd - ref).max() <= 1e-5 * scale
+    oids, _ = orc.search(idx.search_base_lowp(1), q, graph, L=64, k=64, leaf_pids=pids, hits=hits)
+    agree = np.mean([len(set(a[:10]) & set(b[:10])) / 10 for a, b in zip(ids, oids)])
+    assert agree >= 0.98, agree
+    ids2, dd2 = idx.search_projected(q, beam=64, k=64, precision=1, rerank=1)
+    exact = ((base[ids2].astype(np.float64) - q[:, None, :]) ** 2).sum(-1)
+    assert np.allclose(dd2, exact, rtol=1e-5)
+    assert (np.diff(dd2, axis=1) >= 0).all()
+    fp32_ids, _ = orc.search(base, q, graph, L=64, k=64, leaf_pids=pids, hits=hits)
+    gt = ds.ground_truth(base, q, 10)
+    rec_b = ds.recall_at(ids2, gt, 10)
+    rec_f = ds.recall_at(fp32_ids, gt, 10)
+    assert rec_b >= rec_f - 0.01, (rec_b, rec_f)
 
 
 def test_parameter_errors(lib, cuda):
