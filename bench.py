@@ -326,7 +326,9 @@ def main():
         total_s = float(t.item())
     value = nq * args.steps * world / total_s
     head_recall = ds.recall_at(head_ids, w.gt, K_TOP)
+    torch.cuda.nvtx.range_push("rte_timed_plain")
     plain_ms = timed(p_plain, args.steps, args.warmup)
+    torch.cuda.nvtx.range_pop()
     plain_ids = out_ids.cpu().numpy()
     plain_qps = nq * len(plain_ms) / (sum(plain_ms) / 1000.0)
     plain_recall = ds.recall_at(plain_ids, w.gt, K_TOP)
