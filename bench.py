@@ -338,6 +338,13 @@ def main():
     qp = idx.project(qd)
     hits = idx.locate(qp)
 
+    # DRAM bytes (read + write) of one launch of the search kernel on this
+    # workload, from the ncu captures summarised in profiles/ (files
+    # search_kernel_f32_config2_beam32_nq10000.md and
+    # search_kernel_bf16_learned_config2_beam16_nq10000.md).  Only a
+    # configuration that was captured gets a traffic figure.
+    traffic_profiled = {(0, 32): 6.216e9 + 4.6e6, (1, 16): 1.224e9 + 4.4e6}
+
     def kernel_roofline(params, hits_in, elem_bytes, rerank, scale_bytes=0):
         kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                for _ in range(args.steps)]
@@ -355,7 +362,8 @@ def main():
         alg = algorithmic_bytes(cnt, d, params.beam, R, K_TOP, elem_bytes, rerank, scale_bytes)
         ach = alg / (kms / 1000.0) / 1e9
         return {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                "traffic": None, "kernel": "search_kernel", "kernel_ms": kms,
+                "traffic": traffic_profiled.get((params.precision, params.beam)),
+                "kernel": "search_kernel", "kernel_ms": kms,
                 "alg_bytes_per_launch": alg, "peak_kind": hbm_kind,
                 "mean_dist_evals": float(cnt[:, 2].mean()), "mean_expanded": float(cnt[:, 1].mean())}
 
