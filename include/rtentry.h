@@ -297,6 +297,13 @@ rte_status rte_mlp_grad_check(const float* X, const int32_t* labels, int M, int 
 rte_status rte_gemm_bf16(const uint16_t* A, const uint16_t* B, int M, int N, int K, float* C,
                          void* stream);
 
+/* The learned head's last layer alone: for each row m, the column n of the
+ * largest A[m]·B[n] + bias[n] (the first one on ties), through the same
+ * tensor-core kernel and fused argmax epilogue as rte_learned_predict.
+ * Host or device pointers; cols [M] int32.  (No reference counterpart.) */
+rte_status rte_gemm_bf16_bias_argmax(const uint16_t* A, const uint16_t* B, const float* bias, int M,
+                                     int N, int K, int32_t* cols, void* stream);
+
 /* Message of the last failure on this thread ("" if none). */
 const char* rte_last_error(void);
 

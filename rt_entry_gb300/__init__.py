@@ -31,7 +31,7 @@ EXPORTS = (
     "rte_get_kdtree", "rte_index_save", "rte_index_load_dir", "rte_index_free", "rte_last_error",
     "rte_kdtree_build_host", "rte_sym_eig_host", "rte_get_search_base_lowp", "rte_gemm_bf16",
     "rte_default_train_params", "rte_learned_train", "rte_learned_predict", "rte_mlp_grad_check",
-    "rte_search_projected_noalloc", "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
+    "rte_search_projected_noalloc", "rte_gemm_bf16_bias_argmax", "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
     "rte_batcher_free", "rte_autotune",
 )
 
@@ -122,6 +122,7 @@ def load_library(path: str = LIB_PATH):
         "rte_sym_eig_host": ([P, i32, P, P], i32),
         "rte_get_search_base_lowp": ([P, i32, P], i32),
         "rte_gemm_bf16": ([P, P, i32, i32, i32, P, P], i32),
+        "rte_gemm_bf16_bias_argmax": ([P, P, P, i32, i32, i32, P, P], i32),
         "rte_default_train_params": ([ctypes.POINTER(TrainParams)], None),
         "rte_learned_train": ([P, P, i64, ctypes.POINTER(TrainParams), ctypes.POINTER(TrainReport)], i32),
         "rte_learned_predict": ([P, P, i64, P, P], i32),
@@ -228,6 +229,21 @@ def bf16_bits(x):
     """FP32 -> BF16 bit patterns (round to nearest even), as uint16."""
     b = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
     return ((b + 0x7FFF + ((b >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def gemm_bf16_bias_argmax(a_bits, b_bits, bias):
+    """Row argmax of A @ B.T + bias on the tensor cores (the learned head's
+    last layer); A [M,K], B [N,K] BF16 bit patterns, bias [N] FP32."""
+    a = np.ascontiguousarray(a_bits, np.uint16)
+    b = np.ascontiguousarray(b_bits, np.uint16)
+    bias = np.ascontiguousarray(bias, np.float32)
+    M, K = a.shape
+    N = b.shape[0]
+    out = np.empty(M, np.int32)
+    _check(load_library().rte_gemm_bf16_bias_argmax(
+        a.ctypes.data_as(ctypes.c_void_p), b.ctypes.data_as(ctypes.c_void_p),
+        bias.ctypes.data_as(ctypes.c_void_p), M, N, K, out.ctypes.data_as(ctypes.c_void_p), None))
+    return out
 
 
 def gemm_bf16(a_bits, b_bits):

@@ -46,7 +46,7 @@ bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 rte_status learned_leaves(const rte_index* x, const float* d_proj, int64_t nq, int32_t* d_leaf,
-                          cudaStream_t st);
+                          cudaStream_t st, const uint16_t* xb_in = nullptr);
 }  // namespace rte
 
 namespace {
@@ -215,11 +215,22 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   if (s != RTE_OK) return s;
   if (nq == 0) return RTE_OK;
   const float* qp = d_queries;
-  AsyncBuf proj, hitsb, work;
+  AsyncBuf proj, hitsb, work, xb;
+  // learned entries without caller hits: the projection also writes the
+  // model's BF16 input rows
+  const bool head_input = prm->entry_mode == RTE_ENTRY_LEARNED && !d_hits_in && x->mlp.trained &&
+                          x->mlp.d_in == x->search_dim;
   if (!already_projected && x->has_pca) {
     RTE_CUDA(proj.alloc((size_t)nq * x->search_dim * 4, st));
-    RTE_CUDA(launch_project(d_queries, nq, x->dim, x->dim, x->d_mean.p, x->d_rot.p, x->search_dim,
-                            x->search_dim, proj.as<float>(), x->search_dim, st));
+    if (head_input) {
+      RTE_CUDA(xb.alloc((size_t)nq * x->mlp.dp * 2, st));
+      RTE_CUDA(launch_project_bf16(d_queries, nq, x->dim, x->dim, x->d_mean.p, x->d_rot.p,
+                                   x->search_dim, x->search_dim, proj.as<float>(), x->search_dim,
+                                   xb.p, x->mlp.in_scale, x->mlp.dp, st));
+    } else {
+      RTE_CUDA(launch_project(d_queries, nq, x->dim, x->dim, x->d_mean.p, x->d_rot.p,
+                              x->search_dim, x->search_dim, proj.as<float>(), x->search_dim, st));
+    }
     qp = proj.as<float>();
   }
   const int32_t* hits = d_hits_in;
@@ -237,7 +248,8 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
     hits2 = hits2b.as<int32_t>();
     if (!hits) {
       RTE_CUDA(hitsb.alloc((size_t)nq * 4, st));
-      rte_status ls = learned_leaves(x, qp, nq, hitsb.as<int32_t>(), st);
+      rte_status ls = learned_leaves(x, qp, nq, hitsb.as<int32_t>(), st,
+                                     xb.p ? xb.as<uint16_t>() : nullptr);
       if (ls != RTE_OK) return ls;
       hits = hitsb.as<int32_t>();
     }

@@ -31,31 +31,40 @@ namespace rte {
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64;
+constexpr int BM = 128, BK = 64;
 constexpr int A_BYTES = BM * BK * 2;  // one 128 x 64 chunk of A
-constexpr int B_BYTES = BN * BK * 2;  // one 128 x 64 chunk of B
 constexpr int RING_BYTES = 11 * A_BYTES;
-// resident A (K <= 256): 4 A chunks + 7 B stages; streamed: 5 stages of A + B
 constexpr int kResidentChunks = 4;
 constexpr int kResidentK = kResidentChunks * BK;
-constexpr int kStagesResident = (RING_BYTES - kResidentChunks * A_BYTES) / B_BYTES;
-constexpr int kStagesStreamed = RING_BYTES / (A_BYTES + B_BYTES);
-constexpr int kMaxStages = kStagesResident;
+constexpr int kMaxStages = 7;
 constexpr int kChunk = 32;                // accumulator columns per TMEM load
 constexpr int kStageLd = kChunk + 4;      // staging row pitch (floats): conflict-free v4 access
 constexpr int kEpiWarps = 8;             // two per TMEM lane quarter, one per column half
-constexpr int kHalf = BN / 2;
+
+// Output tiles are 128 x BN, BN = 128 or 256 (one MMA instruction covers the
+// whole tile width).  Resident A (K <= 256): 4 A chunks + 7 (BN = 128) or 3
+// (BN = 256) B stages; streamed: 5 or 3 stages of A + B.  Two accumulators
+// of BN columns each: 256 or all 512 TMEM columns.
+template <int BN_>
+struct Tile {
+  static constexpr int BN = BN_;
+  static constexpr int B_BYTES = BN * BK * 2;  // one BN x 64 chunk of B
+  static constexpr int kStagesResident = (RING_BYTES - kResidentChunks * A_BYTES) / B_BYTES;
+  static constexpr int kStagesStreamed = RING_BYTES / (A_BYTES + B_BYTES);
+  static constexpr int kHalf = BN / 2;           // columns per epilogue warp
+  // Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
+  // (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
+  // 17-22, M >> 4 at bits 24-28.
+  static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
+                                     ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+  static_assert(kStagesResident <= kMaxStages && kStagesStreamed <= kMaxStages, "barrier slots");
+};
+
 constexpr int STAGE_BYTES = kEpiWarps * 32 * kStageLd * 4;
 constexpr int SMEM_BYTES = RING_BYTES + STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int kProducerWarp = kEpiWarps, kMmaWarp = kEpiWarps + 1;
 constexpr int kThreads = 32 * (kEpiWarps + 2);
 constexpr long long kWaitLimit = 1ll << 24;  // try_wait rounds before giving up (~seconds)
-
-// Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
-// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
-// 17-22, M >> 4 at bits 24-28.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -118,11 +127,12 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(acc));
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
@@ -149,9 +159,12 @@ __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+template <int BN_>
 __global__ void __launch_bounds__(kThreads, 1)
     gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA,
                         const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
+  using T = Tile<BN_>;
+  constexpr int BN = T::BN, B_BYTES = T::B_BYTES, kHalf = T::kHalf;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* ring = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   float* stage = reinterpret_cast<float*>(ring + RING_BYTES);
@@ -170,7 +183,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int n_tiles = (g.N + BN - 1) / BN;
   const int m_tiles = (g.M + BM - 1) / BM;
   const bool resident = g.K <= kResidentK;
-  const int nst = resident ? kStagesResident : kStagesStreamed;
+  const int nst = resident ? T::kStagesResident : T::kStagesStreamed;
   // this CTA's contiguous range of output tiles, row-block major
   const long long total = (long long)m_tiles * n_tiles;
   const long long t_begin = total * blockIdx.x / gridDim.x;
@@ -279,7 +292,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint64_t bd = sw128_desc(smem_u32(b_addr(s)));
 #pragma unroll
           for (int kk = 0; kk < BK / 16; ++kk)  // +32 bytes per K=16 step inside the swizzle atom
-            mma_bf16(d, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), (kt | kk) != 0);
+            mma_bf16(d, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), T::kIdesc, (kt | kk) != 0);
           mma_commit(empty0 + 8 * s);
         }
         if (!ok) break;
@@ -510,27 +523,36 @@ cudaError_t gemm_bf16_tn(const GemmArgs& g, cudaStream_t st) {
       ((g.epilogue == kEpiBiasArgmax || g.epilogue == kEpiBiasF32 ||
         g.epilogue == kEpiBiasReluBF16) && !g.bias))
     return cudaErrorInvalidValue;
+  // 128 x 256 tiles (half the MMA instructions per FLOP) for the wide
+  // argmax layer, 128 x 128 elsewhere (twice the CTAs for narrow outputs)
+  const bool wide = g.epilogue == kEpiBiasArgmax && g.N >= 1024;
+  const int bn = wide ? 256 : 128;
   CUtensorMap ma, mb;
-  if (!make_map(&ma, g.A, g.M, g.K, BM) || !make_map(&mb, g.B, g.N, g.K, BN))
+  if (!make_map(&ma, g.A, g.M, g.K, BM) || !make_map(&mb, g.B, g.N, g.K, bn))
     return cudaErrorNotSupported;
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(gemm_bf16_tn_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
+  static int num_sms[64] = {0};
+  static bool attr[2][64] = {{false}};
+  if (dev >= 64) return cudaErrorInvalidDevice;
+  if (!attr[wide][dev]) {
+    cudaError_t e = wide ? cudaFuncSetAttribute(gemm_bf16_tn_kernel<256>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES)
+                         : cudaFuncSetAttribute(gemm_bf16_tn_kernel<128>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    attr = true;
+    attr[wide][dev] = true;
   }
   // one CTA per SM, each taking a contiguous range of the output tiles
-  static int num_sms = 0;
-  if (num_sms == 0) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      num_sms = 1;
-  }
-  const long long tiles = (long long)((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN);
-  dim3 grid((unsigned)(tiles < num_sms ? tiles : num_sms));
-  gemm_bf16_tn_kernel<<<grid, kThreads, SMEM_BYTES, st>>>(ma, mb, g);
+  if (num_sms[dev] == 0 &&
+      cudaDeviceGetAttribute(&num_sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    num_sms[dev] = 1;
+  const long long tiles = (long long)((g.M + BM - 1) / BM) * ((g.N + bn - 1) / bn);
+  dim3 grid((unsigned)(tiles < num_sms[dev] ? tiles : num_sms[dev]));
+  if (wide)
+    gemm_bf16_tn_kernel<256><<<grid, kThreads, SMEM_BYTES, st>>>(ma, mb, g);
+  else
+    gemm_bf16_tn_kernel<128><<<grid, kThreads, SMEM_BYTES, st>>>(ma, mb, g);
   return cudaGetLastError();
 }
 

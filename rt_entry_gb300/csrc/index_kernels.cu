@@ -117,7 +117,9 @@ __global__ void __launch_bounds__(128) project_rows(const float* __restrict__ x,
                                                     int xstride, const float* __restrict__ mean,
                                                     const float* __restrict__ V, int vstride, int k,
                                                     float* __restrict__ out, int ostride,
-                                                    const int* __restrict__ n_dev) {
+                                                    const int* __restrict__ n_dev,
+                                                    __nv_bfloat16* __restrict__ out16, float s16,
+                                                    int ld16) {
   if (n_dev) n = min(n, (int64_t)*n_dev);  // graph replay: rows beyond the batch are idle
   if ((int64_t)blockIdx.x * kPrRows >= n) return;
   __shared__ float sx[kPrRows][kPrK + 1];
@@ -172,6 +174,9 @@ __global__ void __launch_bounds__(128) project_rows(const float* __restrict__ x,
     for (int j = 0; j < 4; ++j) {
       const int col = col0 + 4 * tx + j;
       if (col < k) out[r * ostride + col] = acc[i][j];
+      // the learned head's input: value * scale rounded to BF16, zero in the
+      // padding columns k .. ld16-1 (acc is 0 there)
+      if (out16 && col < ld16) out16[r * ld16 + col] = __float2bfloat16_rn(__fmul_rn(acc[i][j], s16));
     }
   }
 }
@@ -304,12 +309,14 @@ __global__ void locate_points(const BvhNode* __restrict__ nodes, int n_nodes,
 // Used by the learned entry, whose model predicts the subtree.
 __global__ void locate_in_subtree(const BvhNode* __restrict__ nodes, const float* __restrict__ pts,
                                   int64_t n, int stride, const int32_t* __restrict__ cls,
+                                  const unsigned long long* __restrict__ keys,
                                   const int32_t* __restrict__ start_node,
                                   const int32_t* __restrict__ fallback_leaf,
                                   int32_t* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int c = cls[i];
+  // the class is given, or decoded from the packed argmax key (gemm_tc.h)
+  const int c = keys ? 0x7fffffff - (int)(keys[i] & 0xffffffffu) : cls[i];
   const float x = pts[i * stride + 0], y = pts[i * stride + 1], z = pts[i * stride + 2];
   int stack[kBvhMaxDepth];
   int sp = 0;
@@ -352,11 +359,13 @@ __global__ void bf16_norms(const uint16_t* __restrict__ il16, int64_t n, int C,
 
 // -------------------------------------------------------------- launches ----
 cudaError_t launch_locate_in_subtree(const BvhNode* nodes, const float* pts, int64_t n, int stride,
-                                     const int32_t* cls, const int32_t* start_node,
-                                     const int32_t* fallback_leaf, int32_t* out, cudaStream_t st) {
+                                     const int32_t* cls, const unsigned long long* keys,
+                                     const int32_t* start_node, const int32_t* fallback_leaf,
+                                     int32_t* out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  locate_in_subtree<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(nodes, pts, n, stride, cls,
-                                                                  start_node, fallback_leaf, out);
+  if (!cls == !keys) return cudaErrorInvalidValue;
+  locate_in_subtree<<<(unsigned)((n + 63) / 64), 64, 0, st>>>(nodes, pts, n, stride, cls, keys,
+                                                                start_node, fallback_leaf, out);
   return cudaGetLastError();
 }
 
@@ -383,7 +392,19 @@ cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const 
                            cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  project_rows<<<grid, 128, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr);
+  project_rows<<<grid, 128, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr,
+                                     nullptr, 0.0f, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_project_bf16(const float* x, int64_t n, int d, int xstride, const float* mean,
+                                const float* V, int vstride, int k, float* out, int ostride,
+                                void* out16, float s16, int ld16, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  if (ld16 < k || ld16 > ((k + kPrCols - 1) / kPrCols) * kPrCols) return cudaErrorInvalidValue;
+  dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
+  project_rows<<<grid, 128, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr,
+                                     reinterpret_cast<__nv_bfloat16*>(out16), s16, ld16);
   return cudaGetLastError();
 }
 
@@ -391,7 +412,8 @@ cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, in
                                const float* mean, const float* V, int vstride, int k, float* out,
                                int ostride, cudaStream_t st) {
   dim3 grid((unsigned)((cap + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  project_rows<<<grid, 128, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride, n_dev);
+  project_rows<<<grid, 128, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride, n_dev,
+                                     nullptr, 0.0f, 0);
   return cudaGetLastError();
 }
 

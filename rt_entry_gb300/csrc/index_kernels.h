@@ -26,6 +26,12 @@ cudaError_t launch_cov(const float* x, int64_t n, int d, const double* mean, dou
 cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const float* mean,
                            const float* V, int vstride, int k, float* out, int ostride,
                            cudaStream_t st);
+// launch_project plus a BF16 copy of the output: out16[r][c] =
+// bf16(out[r][c] * s16) for c < k, 0 for k <= c < ld16 (the learned head's
+// input rows, ld16 >= k).
+cudaError_t launch_project_bf16(const float* x, int64_t n, int d, int xstride, const float* mean,
+                                const float* V, int vstride, int k, float* out, int ostride,
+                                void* out16, float s16, int ld16, cudaStream_t st);
 // Variants for graph replay: grids sized for `cap` rows, the live row count
 // read from device memory at run time.
 cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, int d, int xstride,
@@ -42,9 +48,12 @@ cudaError_t launch_deinterleave(const float* il32, int64_t n, int d, int C, floa
 cudaError_t launch_bf16_norms(const uint16_t* il16, int64_t n, int C, float* out, cudaStream_t st);
 cudaError_t launch_dequant(const void* il, const float* scale8, int precision, int64_t n, int d,
                            int C, float* dst, cudaStream_t st);
+// The class of point i is cls[i], or decoded from the packed argmax key
+// keys[i] (exactly one of the two is given).
 cudaError_t launch_locate_in_subtree(const BvhNode* nodes, const float* pts, int64_t n, int stride,
-                                     const int32_t* cls, const int32_t* start_node,
-                                     const int32_t* fallback_leaf, int32_t* out, cudaStream_t st);
+                                     const int32_t* cls, const unsigned long long* keys,
+                                     const int32_t* start_node, const int32_t* fallback_leaf,
+                                     int32_t* out, cudaStream_t st);
 cudaError_t launch_locate(const BvhNode* nodes, int n_nodes, const float* pts, int64_t n, int stride,
                           int32_t* out, cudaStream_t st);
 

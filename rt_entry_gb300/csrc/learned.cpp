@@ -61,6 +61,63 @@ extern "C" rte_status rte_gemm_bf16(const uint16_t* A, const uint16_t* B, int M,
   return RTE_OK;
 }
 
+extern "C" rte_status rte_gemm_bf16_bias_argmax(const uint16_t* A, const uint16_t* B,
+                                                const float* bias, int M, int N, int K,
+                                                int32_t* cols, void* stream) {
+  clear_error();
+  if (!A || !B || !bias || !cols || M <= 0 || N <= 0 || K <= 0)
+    return fail(RTE_EINVAL, "bad GEMM arguments");
+  if (K % 8) return fail(RTE_EINVAL, "K must be a multiple of 8");
+  cudaStream_t st = (cudaStream_t)stream;
+  AsyncBuf a, b, bb, keys, out, e;
+  const void* pa = A;
+  const void* pb = B;
+  const float* pbias = bias;
+  if (!is_device_ptr(A)) {
+    RTE_CUDA(a.alloc((size_t)M * K * 2, st));
+    RTE_CUDA(cudaMemcpyAsync(a.p, A, (size_t)M * K * 2, cudaMemcpyHostToDevice, st));
+    pa = a.p;
+  }
+  if (!is_device_ptr(B)) {
+    RTE_CUDA(b.alloc((size_t)N * K * 2, st));
+    RTE_CUDA(cudaMemcpyAsync(b.p, B, (size_t)N * K * 2, cudaMemcpyHostToDevice, st));
+    pb = b.p;
+  }
+  if (!is_device_ptr(bias)) {
+    RTE_CUDA(bb.alloc((size_t)N * 4, st));
+    RTE_CUDA(cudaMemcpyAsync(bb.p, bias, (size_t)N * 4, cudaMemcpyHostToDevice, st));
+    pbias = bb.as<float>();
+  }
+  const bool cd = is_device_ptr(cols);
+  RTE_CUDA(keys.alloc((size_t)M * 8, st));
+  RTE_CUDA(cudaMemsetAsync(keys.p, 0, (size_t)M * 8, st));
+  RTE_CUDA(e.alloc(4, st));
+  RTE_CUDA(cudaMemsetAsync(e.p, 0, 4, st));
+  int32_t* pc = cols;
+  if (!cd) {
+    RTE_CUDA(out.alloc((size_t)M * 4, st));
+    pc = out.as<int32_t>();
+  }
+  GemmArgs g{};
+  g.A = pa;
+  g.B = pb;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.epilogue = kEpiBiasArgmax;
+  g.bias = pbias;
+  g.out_argmax = keys.as<unsigned long long>();
+  g.err = e.as<int>();
+  RTE_CUDA(gemm_bf16_tn(g, st));
+  RTE_CUDA(launch_argmax_to_leaf(keys.as<unsigned long long>(), M, nullptr, pc, st));
+  int herr = 0;
+  RTE_CUDA(cudaMemcpyAsync(&herr, e.p, 4, cudaMemcpyDeviceToHost, st));
+  if (!cd) RTE_CUDA(cudaMemcpyAsync(cols, pc, (size_t)M * 4, cudaMemcpyDeviceToHost, st));
+  RTE_CUDA(cudaStreamSynchronize(st));
+  if (herr) return fail(RTE_ETIMEOUT, "GEMM pipeline wait ran out (code " + std::to_string(herr) + ")");
+  return RTE_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Learned entry.  A 3-layer MLP (search-space query -> hidden -> hidden ->
 // kd-tree leaf) proposes the entry leaf.  It is trained on (query, leaf of
@@ -96,21 +153,31 @@ cudaError_t gemm(const void* A, const void* B, int M, int N, int K, int epi, voi
 
 int round8(int v) { return (v + 7) & ~7; }
 
-// MLP forward for nq rows of X (BF16 [nq x dp]) -> class (subtree) per row.
-rte_status mlp_predict_bf16(const rte_index* x, const uint16_t* X, int64_t nq, int32_t* d_cls,
-                            int* d_err, cudaStream_t st) {
+// MLP forward for nq rows of X (BF16 [nq x dp]) -> packed argmax key per row
+// (keys [nq], zeroed here).
+rte_status mlp_keys_bf16(const rte_index* x, const uint16_t* X, int64_t nq, unsigned long long* keys,
+                         int* d_err, cudaStream_t st) {
   const Mlp& m = x->mlp;
-  AsyncBuf h1, h2, keys;
+  AsyncBuf h1, h2;
   RTE_CUDA(h1.alloc((size_t)nq * m.hidden * 2, st));
   RTE_CUDA(h2.alloc((size_t)nq * m.hidden * 2, st));
-  RTE_CUDA(keys.alloc((size_t)nq * 8, st));
-  RTE_CUDA(cudaMemsetAsync(keys.p, 0, (size_t)nq * 8, st));
+  RTE_CUDA(cudaMemsetAsync(keys, 0, (size_t)nq * 8, st));
   RTE_CUDA(gemm(X, m.W16[0].p, (int)nq, m.hidden, m.dp, kEpiBiasReluBF16, h1.p, m.hidden, m.b[0].p,
                 nullptr, d_err, st));
   RTE_CUDA(gemm(h1.p, m.W16[1].p, (int)nq, m.hidden, m.hidden, kEpiBiasReluBF16, h2.p, m.hidden,
                 m.b[1].p, nullptr, d_err, st));
   RTE_CUDA(gemm(h2.p, m.W16[2].p, (int)nq, m.classes, m.hidden, kEpiBiasArgmax, nullptr, 0,
-                m.b[2].p, keys.as<unsigned long long>(), d_err, st));
+                m.b[2].p, keys, d_err, st));
+  return RTE_OK;
+}
+
+// MLP forward for nq rows of X (BF16 [nq x dp]) -> class (subtree) per row.
+rte_status mlp_predict_bf16(const rte_index* x, const uint16_t* X, int64_t nq, int32_t* d_cls,
+                            int* d_err, cudaStream_t st) {
+  AsyncBuf keys;
+  RTE_CUDA(keys.alloc((size_t)nq * 8, st));
+  rte_status s = mlp_keys_bf16(x, X, nq, keys.as<unsigned long long>(), d_err, st);
+  if (s != RTE_OK) return s;
   RTE_CUDA(launch_argmax_to_leaf(keys.as<unsigned long long>(), (int)nq, nullptr, d_cls, st));
   return RTE_OK;
 }
@@ -217,23 +284,30 @@ rte_status fwd_bwd(const Mlp& m, const uint16_t* Xb, const int32_t* yb, int M, S
 namespace rte {
 
 // Leaf prediction for projected queries already on the device.
+// xb: the head's BF16 input rows ([nq x dp], from launch_project_bf16), or
+// null to form them here from d_proj.
 rte_status learned_leaves(const rte_index* x, const float* d_proj, int64_t nq, int32_t* d_leaf,
-                          cudaStream_t st) {
+                          cudaStream_t st, const uint16_t* xb_in) {
   if (!x->mlp.trained) return fail(RTE_ESTATE, "learned entries requested before rte_learned_train");
   if (nq == 0) return RTE_OK;
   const Mlp& m = x->mlp;
-  AsyncBuf xb, err;
-  RTE_CUDA(xb.alloc((size_t)nq * m.dp * 2, st));
+  AsyncBuf xb, err, keys;
   RTE_CUDA(err.alloc(4, st));
   RTE_CUDA(cudaMemsetAsync(err.p, 0, 4, st));
-  RTE_CUDA(launch_cast_rows_bf16(d_proj, nq, m.d_in, x->search_dim, m.in_scale, m.dp, xb.p, st));
-  AsyncBuf cls;
-  RTE_CUDA(cls.alloc((size_t)nq * 4, st));
-  rte_status s = mlp_predict_bf16(x, xb.as<uint16_t>(), nq, cls.as<int32_t>(), err.as<int>(), st);
+  const uint16_t* X = xb_in;
+  if (!X) {
+    RTE_CUDA(xb.alloc((size_t)nq * m.dp * 2, st));
+    RTE_CUDA(launch_cast_rows_bf16(d_proj, nq, m.d_in, x->search_dim, m.in_scale, m.dp, xb.p, st));
+    X = xb.as<uint16_t>();
+  }
+  RTE_CUDA(keys.alloc((size_t)nq * 8, st));
+  rte_status s = mlp_keys_bf16(x, X, nq, keys.as<unsigned long long>(), err.as<int>(), st);
   if (s != RTE_OK) return s;
-  // the model picks the subtree, the kd-tree picks the leaf inside it
-  RTE_CUDA(launch_locate_in_subtree(x->d_nodes.p, d_proj, nq, x->search_dim, cls.as<int32_t>(),
-                                    m.class_node.p, m.class_leaf0.p, d_leaf, st));
+  // the model picks the subtree (decoded from its argmax key), the kd-tree
+  // picks the leaf inside it
+  RTE_CUDA(launch_locate_in_subtree(x->d_nodes.p, d_proj, nq, x->search_dim, nullptr,
+                                    keys.as<unsigned long long>(), m.class_node.p, m.class_leaf0.p,
+                                    d_leaf, st));
   return RTE_OK;
 }
 
@@ -472,7 +546,7 @@ extern "C" rte_status rte_learned_predict(rte_index* x, const float* projected, 
     RTE_CUDA(ob.alloc((size_t)nq * 4, st));
     dout = ob.as<int32_t>();
   }
-  rte_status s = learned_leaves(x, dp, nq, dout, st);
+  rte_status s = learned_leaves(x, dp, nq, dout, st, nullptr);
   if (s != RTE_OK) return s;
   if (host_out) {
     RTE_CUDA(cudaMemcpyAsync(out_leaf, dout, (size_t)nq * 4, cudaMemcpyDeviceToHost, st));

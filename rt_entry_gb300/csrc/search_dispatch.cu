@@ -1,6 +1,10 @@
 // search_dispatch.cu -- maps (chunks, precision) to the instantiation files.
 #include "search_dispatch.h"
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 namespace rte {
 
 void* search_lookup_c1_f32(int, int);
@@ -60,6 +64,17 @@ cudaError_t launch_search(const SearchArgs& a, int C, int NL, int NB, int prec, 
 int occupancy_search(int C, int NL, int NB, int prec, int wpb, size_t smem) {
   void* k = search_kernel_ptr(C, NL, NB, prec);
   if (!k) return 0;
+  // the answer depends only on (kernel, device, block, shared memory): cache it
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  static std::mutex mu;
+  static std::map<std::tuple<void*, int, int, size_t>, int> cache;
+  const auto key = std::make_tuple(k, dev, wpb, smem);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
@@ -68,6 +83,8 @@ int occupancy_search(int C, int NL, int NB, int prec, int wpb, size_t smem) {
     cudaGetLastError();
     return 0;
   }
+  std::lock_guard<std::mutex> lock(mu);
+  cache[key] = n;
   return n;
 }
 

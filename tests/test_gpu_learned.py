@@ -25,6 +25,37 @@ def test_tensor_core_gemm_matches_fp64(lib, cuda):
         assert np.abs(c - ref).max() <= 1e-5 * np.abs(ref).max(), (M, N, K)
 
 
+def test_tensor_core_bias_argmax_matches_fp64(lib, cuda):
+    """The fused bias + row-argmax epilogue of the head's last layer: 128 x
+    256 tiles for wide outputs (resident and streamed A), 128 x 128 for
+    narrow ones.  The chosen column's value must be the FP64 maximum within
+    the FP32 accumulation error, and equal columns must resolve to the
+    first one."""
+    import rt_entry_gb300 as r
+    rng = np.random.default_rng(5)
+    for M, N, K in [(10000, 4096, 256), (3000, 2048, 320), (700, 1030, 128), (500, 300, 64)]:
+        a = rng.standard_normal((M, K)).astype(np.float32)
+        b = rng.standard_normal((N, K)).astype(np.float32)
+        bias = rng.standard_normal(N).astype(np.float32)
+        ab, bb = r.bf16_bits(a), r.bf16_bits(b)
+        af = (ab.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+        bf = (bb.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+        logits = af @ bf.T + bias
+        cols = r.gemm_bf16_bias_argmax(ab, bb, bias)
+        assert ((cols >= 0) & (cols < N)).all(), (M, N, K)
+        best = logits.max(1)
+        got = logits[np.arange(M), cols]
+        assert (best - got).max() <= 1e-5 * np.abs(logits).max(), (M, N, K)
+        assert (cols == logits.argmax(1)).mean() > 0.999, (M, N, K)
+    # ties: duplicated columns of B -> the first index wins
+    M, N, K = 256, 1536, 64
+    a = rng.standard_normal((M, K)).astype(np.float32)
+    b = rng.standard_normal((N, K)).astype(np.float32)
+    b[N // 2:] = b[: N // 2]
+    cols = r.gemm_bf16_bias_argmax(r.bf16_bits(a), r.bf16_bits(b), np.zeros(N, np.float32))
+    assert (cols < N // 2).all()
+
+
 def test_mlp_gradients_match_oracle(lib, cuda):
     import rt_entry_gb300 as r
     from oracle import mlp_ref
@@ -78,7 +109,11 @@ def test_learned_entry_trains_and_searches(lib, orc, cuda):
                           hits2=kd)
     assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
     assert np.array_equal(dd, od)
-    # beam 16: eight entries from each leaf
+    # raw queries (the projection also writes the model's BF16 input) give
+    # the same learned search as projected ones (a separate cast)
+    ir, dr = idx.search(q, beam=64, k=64, entry_mode=r.ENTRY_LEARNED)
+    assert np.array_equal(ir, ids) and np.array_equal(dr, dd)
+    # beam 16: both whole leaves as entries
     ids, dd = idx.search_projected(qp, beam=16, k=16, entry_mode=r.ENTRY_LEARNED)
     oids, od = orc.search(pb, qp, graph, L=16, k=16, entry_mode=2, leaf_pids=pids, hits=learned,
                           hits2=kd)
