@@ -54,7 +54,7 @@ namespace {
 size_t index_bytes(const rte_index* x) {
   return x->raw.bytes() + x->graph.bytes() + x->d_mean.bytes() + x->d_rot.bytes() +
          x->il32.bytes() + x->il16.bytes() + x->il8.bytes() + x->scale8.bytes() + x->norm16.bytes() +
-         x->d_nodes.bytes() + x->d_pids.bytes();
+         x->d_nodes.bytes() + x->d_wide.bytes() + x->d_pids.bytes();
 }
 
 // (Re)build the lane-interleaved FP32/BF16/FP8 copies of the search space
@@ -79,6 +79,7 @@ rte_status make_search_space(rte_index* x, const float* rm) {
   // a new search space invalidates the kd-tree built on the old one
   x->has_kdtree = false;
   x->d_nodes.reset();
+  x->d_wide.reset();
   x->d_pids.reset();
   return RTE_OK;
 }
@@ -238,13 +239,13 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   AsyncBuf hits2b;
   if (prm->entry_mode == RTE_ENTRY_KDTREE && !hits) {
     RTE_CUDA(hitsb.alloc((size_t)nq * 4, st));
-    RTE_CUDA(launch_locate(x->d_nodes.p, (int)x->d_nodes.n, qp, nq, x->search_dim, hitsb.as<int32_t>(), st));
+    RTE_CUDA(launch_locate(x->d_wide.p, (int)x->d_wide.n, qp, nq, x->search_dim, hitsb.as<int32_t>(), st));
     hits = hitsb.as<int32_t>();
   }
   if (prm->entry_mode == RTE_ENTRY_LEARNED) {
     // proposed leaf (MLP) first, kd-tree leaf second
     RTE_CUDA(hits2b.alloc((size_t)nq * 4, st));
-    RTE_CUDA(launch_locate(x->d_nodes.p, (int)x->d_nodes.n, qp, nq, x->search_dim, hits2b.as<int32_t>(), st));
+    RTE_CUDA(launch_locate(x->d_wide.p, (int)x->d_wide.n, qp, nq, x->search_dim, hits2b.as<int32_t>(), st));
     hits2 = hits2b.as<int32_t>();
     if (!hits) {
       RTE_CUDA(hitsb.alloc((size_t)nq * 4, st));
@@ -437,6 +438,10 @@ rte_status rte_build_kdtree(rte_index* x, int leaf_size, float expand_ratio) {
   kd_expand(t, expand_ratio);
   RTE_CUDA(x->d_nodes.alloc(t.nodes.size()));
   RTE_CUDA(cudaMemcpy(x->d_nodes.p, t.nodes.data(), x->d_nodes.bytes(), cudaMemcpyHostToDevice));
+  std::vector<WideNode> wide;
+  kd_wide(t, wide);
+  RTE_CUDA(x->d_wide.alloc(wide.size()));
+  RTE_CUDA(cudaMemcpy(x->d_wide.p, wide.data(), x->d_wide.bytes(), cudaMemcpyHostToDevice));
   RTE_CUDA(x->d_pids.alloc(t.pids.size()));
   RTE_CUDA(cudaMemcpy(x->d_pids.p, t.pids.data(), x->d_pids.bytes(), cudaMemcpyHostToDevice));
   x->kd = std::move(t);
@@ -500,7 +505,7 @@ rte_status rte_locate(rte_index* x, const float* projected, int64_t nq, int32_t*
     RTE_CUDA(ob.alloc((size_t)nq * 4, st));
     dout = ob.as<int32_t>();
   }
-  RTE_CUDA(launch_locate(x->d_nodes.p, (int)x->d_nodes.n, dp, nq, x->search_dim, dout, st));
+  RTE_CUDA(launch_locate(x->d_wide.p, (int)x->d_wide.n, dp, nq, x->search_dim, dout, st));
   if (!od) {
     RTE_CUDA(cudaMemcpyAsync(out_leaf, dout, (size_t)nq * 4, cudaMemcpyDeviceToHost, st));
     RTE_CUDA(cudaStreamSynchronize(st));

@@ -196,6 +196,56 @@ bool kd_build(const float* xyz, int64_t n, int cap, KdTree& out, std::string& er
   return true;
 }
 
+void kd_wide(const KdTree& t, std::vector<WideNode>& out) {
+  out.clear();
+  std::vector<int> start{0};  // binary node that each wide node expands, breadth-first
+  std::vector<int> kids;
+  for (size_t h = 0; h < start.size(); ++h) {
+    const int b = start[h];
+    kids.clear();
+    if (t.nodes[b].left < 0) {
+      kids.push_back(b);  // a tree that is one leaf
+    } else {
+      // pre-order, left first: descendants 3 levels down, or leaves met before
+      std::vector<std::pair<int, int>> st{{t.nodes[b].right, 1}, {t.nodes[b].left, 1}};
+      while (!st.empty()) {
+        auto [k, rel] = st.back();
+        st.pop_back();
+        const BvhNode& nd = t.nodes[k];
+        if (nd.left < 0 || rel == 3) {
+          kids.push_back(k);
+        } else {
+          st.push_back({nd.right, rel + 1});
+          st.push_back({nd.left, rel + 1});
+        }
+      }
+    }
+    WideNode w;
+    for (int c = 0; c < kWide; ++c) {
+      for (int a = 0; a < 3; ++a) {
+        w.lo[a][c] = 3.402823466e38f;
+        w.hi[a][c] = -3.402823466e38f;
+      }
+      w.child[c] = 0;
+      w.pad[c] = 0;
+    }
+    for (size_t c = 0; c < kids.size(); ++c) {
+      const BvhNode& nd = t.nodes[kids[c]];
+      for (int a = 0; a < 3; ++a) {
+        w.lo[a][c] = nd.lo[a];
+        w.hi[a][c] = nd.hi[a];
+      }
+      if (nd.left < 0) {
+        w.child[c] = nd.left;  // -(leaf + 1)
+      } else {
+        w.child[c] = (int32_t)start.size();
+        start.push_back(kids[c]);
+      }
+    }
+    out.push_back(w);
+  }
+}
+
 void kd_expand(KdTree& t, float ratio) {
   t.expanded = t.tight;
   for (int64_t i = 0; i < t.n_leaves; ++i) {

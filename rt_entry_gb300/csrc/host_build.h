@@ -23,6 +23,10 @@ struct KdTree {
   int depth = 0;
 };
 
+// The 8-wide copy of the tree for point location (index_kernels.h), built
+// from the expanded node bounds (call after kd_expand).
+void kd_wide(const KdTree& t, std::vector<WideNode>& out);
+
 // Returns false (with err) when a split leaves one side empty (the
 // reference exits the process there, kdtree.cpp:182-185).
 bool kd_build(const float* xyz, int64_t n, int cap, KdTree& out, std::string& err);

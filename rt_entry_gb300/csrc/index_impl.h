@@ -138,6 +138,7 @@ struct rte_index {
   rte::KdTree kd;
   float expand_ratio = 0.f;
   rte::DevBuf<rte::BvhNode> d_nodes;
+  rte::DevBuf<rte::WideNode> d_wide;  // 8-wide copy for point location
   rte::DevBuf<int32_t> d_pids;
   // learned entry
   rte::Mlp mlp;

@@ -108,11 +108,16 @@ __global__ void cov_finish(const double* __restrict__ partial, int nchunks, int 
 // ---------------------------------------------------------- projection ----
 // out[r][j] = sum_c (x[r][c] - mean[c]) * V[c][j], one fmaf per c in
 // ascending order.  A block computes a 32 x 128 tile; each thread an 8 x 4
-// register tile, so every shared-memory read feeds 4 (x) or 8 (V) FMAs.
+// register tile, so every shared-memory read feeds 4 (x) or 8 (V) FMAs.  The
+// 32-wide slices of c are double-buffered: the next slice's global loads are
+// in flight while the current one is multiplied.  With kOut16 the block also
+// writes the learned head's BF16 input row: bf16(out * s16), zero-padded to
+// ld16 columns.
 constexpr int kPrRows = 32;
 constexpr int kPrCols = 128;
 constexpr int kPrK = 32;
 
+template <bool kOut16>
 __global__ void __launch_bounds__(128) project_rows(const float* __restrict__ x, int64_t n, int d,
                                                     int xstride, const float* __restrict__ mean,
                                                     const float* __restrict__ V, int vstride, int k,
@@ -122,49 +127,68 @@ __global__ void __launch_bounds__(128) project_rows(const float* __restrict__ x,
                                                     int ld16) {
   if (n_dev) n = min(n, (int64_t)*n_dev);  // graph replay: rows beyond the batch are idle
   if ((int64_t)blockIdx.x * kPrRows >= n) return;
-  __shared__ float sx[kPrRows][kPrK + 1];
-  __shared__ __align__(16) float sv[kPrK][kPrCols];
+  __shared__ float sx[2][kPrRows][kPrK + 1];
+  __shared__ __align__(16) float sv[2][kPrK][kPrCols];
   const int64_t row0 = (int64_t)blockIdx.x * kPrRows;
   const int col0 = blockIdx.y * kPrCols;
   const int tx = threadIdx.x & 31;  // columns 4tx .. 4tx+3
   const int ty = threadIdx.x >> 5;  // rows 8ty .. 8ty+7
-  float acc[8][4];
+  constexpr int kXPer = kPrRows * kPrK / 128, kVPer = kPrK * kPrCols / 128;
+  float rx[kXPer], rv[kVPer];
+  auto gload = [&](int c0) {
 #pragma unroll
-  for (int i = 0; i < 8; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
-  for (int c0 = 0; c0 < d; c0 += kPrK) {
-#pragma unroll
-    for (int u = 0; u < kPrRows * kPrK / 128; ++u) {
+    for (int u = 0; u < kXPer; ++u) {
       const int t = threadIdx.x + 128 * u;
       const int rr = t / kPrK, cc = t % kPrK;
       const int64_t r = row0 + rr;
       float v = 0.0f;
       if (r < n && c0 + cc < d) v = __fsub_rn(x[r * xstride + c0 + cc], mean ? mean[c0 + cc] : 0.0f);
-      sx[rr][cc] = v;
+      rx[u] = v;
     }
-#pragma unroll 4
-    for (int u = 0; u < kPrK * kPrCols / 128; ++u) {
-      const int t = threadIdx.x + 128 * u;
-      const int cc = t / kPrCols, jj = t % kPrCols;
+#pragma unroll
+    for (int u = 0; u < kVPer; ++u) {
+      const int cc = u, jj = threadIdx.x;  // t = threadIdx.x + 128u over a 32 x 128 slice
       float v = 0.0f;
       if (c0 + cc < d && col0 + jj < k) v = V[(int64_t)(c0 + cc) * vstride + col0 + jj];
-      sv[cc][jj] = v;
+      rv[u] = v;
     }
-    __syncthreads();
+  };
+  auto sstore = [&](int b) {
+#pragma unroll
+    for (int u = 0; u < kXPer; ++u) {
+      const int t = threadIdx.x + 128 * u;
+      sx[b][t / kPrK][t % kPrK] = rx[u];
+    }
+#pragma unroll
+    for (int u = 0; u < kVPer; ++u) sv[b][u][threadIdx.x] = rv[u];
+  };
+  float acc[8][4];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+  gload(0);
+  sstore(0);
+  __syncthreads();
+  int b = 0;
+  for (int c0 = 0; c0 < d; c0 += kPrK) {
+    const bool more = c0 + kPrK < d;
+    if (more) gload(c0 + kPrK);
 #pragma unroll 8
     for (int cc = 0; cc < kPrK; ++cc) {
-      const float4 v = *reinterpret_cast<const float4*>(&sv[cc][4 * tx]);
+      const float4 v = *reinterpret_cast<const float4*>(&sv[b][cc][4 * tx]);
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
-        const float xv = sx[8 * ty + i][cc];
+        const float xv = sx[b][8 * ty + i][cc];
         acc[i][0] = __fmaf_rn(xv, v.x, acc[i][0]);
         acc[i][1] = __fmaf_rn(xv, v.y, acc[i][1]);
         acc[i][2] = __fmaf_rn(xv, v.z, acc[i][2]);
         acc[i][3] = __fmaf_rn(xv, v.w, acc[i][3]);
       }
     }
+    if (more) sstore(b ^ 1);
     __syncthreads();
+    b ^= 1;
   }
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
@@ -174,9 +198,8 @@ __global__ void __launch_bounds__(128) project_rows(const float* __restrict__ x,
     for (int j = 0; j < 4; ++j) {
       const int col = col0 + 4 * tx + j;
       if (col < k) out[r * ostride + col] = acc[i][j];
-      // the learned head's input: value * scale rounded to BF16, zero in the
-      // padding columns k .. ld16-1 (acc is 0 there)
-      if (out16 && col < ld16) out16[r * ld16 + col] = __float2bfloat16_rn(__fmul_rn(acc[i][j], s16));
+      // acc is 0 in the padding columns k .. ld16-1
+      if (kOut16 && col < ld16) out16[r * ld16 + col] = __float2bfloat16_rn(__fmul_rn(acc[i][j], s16));
     }
   }
 }
@@ -257,48 +280,64 @@ __global__ void dequant_rows(const void* __restrict__ il, const float* __restric
 // the union of its leaves' expanded boxes.  Leaves are numbered in the same
 // order, so the first leaf whose box contains the point is the smallest such
 // index (canonical rule for the ray cast's arbitrary hit).
-// The first kTopNodes nodes (breadth-first numbering: the top ten levels)
-// are copied into shared memory by every block; deeper nodes are read from
-// global memory.
-constexpr int kTopNodes = 1023;
+// Point location on the 8-wide tree: a depth-first search whose stack holds
+// references to containing children, pushed last-first so that children pop
+// in pre-order; the first leaf popped is the smallest containing leaf (every
+// ancestor of a containing leaf contains the point, because node bounds are
+// unions).  The first kTopWide wide nodes (breadth-first: the top three wide
+// levels, nine binary levels) are copied into shared memory by every block.
+constexpr int kTopWide = 73;
+constexpr int kLocStack = 64;
 
-__device__ __forceinline__ void load_top_nodes(const BvhNode* __restrict__ nodes, int n_nodes,
-                                               BvhNode* top) {
-  const int ntop = min(kTopNodes, n_nodes);
-  const float4* src = reinterpret_cast<const float4*>(nodes);
-  float4* dst = reinterpret_cast<float4*>(top);
-  for (int i = threadIdx.x; i < 2 * ntop; i += blockDim.x) dst[i] = __ldg(src + i);
-  __syncthreads();
-}
-
-__global__ void locate_points(const BvhNode* __restrict__ nodes, int n_nodes,
+__global__ void locate_points(const WideNode* __restrict__ wide, int n_wide,
                               const float* __restrict__ pts, int64_t n, int stride,
                               int32_t* __restrict__ out, const int* __restrict__ n_dev) {
-  __shared__ BvhNode top[kTopNodes];
+  __shared__ WideNode top[kTopWide];
   if (n_dev) n = min(n, (int64_t)*n_dev);
   if ((int64_t)blockIdx.x * blockDim.x >= n) return;
-  load_top_nodes(nodes, n_nodes, top);
-  const int ntop = min(kTopNodes, n_nodes);
+  const int ntop = min(kTopWide, n_wide);
+  {
+    const float4* src = reinterpret_cast<const float4*>(wide);
+    float4* dst = reinterpret_cast<float4*>(top);
+    for (int i = threadIdx.x; i < 16 * ntop; i += blockDim.x) dst[i] = __ldg(src + i);
+    __syncthreads();
+  }
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float x = pts[i * stride + 0], y = pts[i * stride + 1], z = pts[i * stride + 2];
-  int stack[kBvhMaxDepth];
+  int stack[kLocStack];
   int sp = 0;
   stack[sp++] = 0;
   int32_t hit = 0;
   while (sp > 0) {
-    const int k = stack[--sp];
-    const BvhNode nd = k < ntop ? top[k] : nodes[k];
-    if (!(nd.lo[0] <= x && x <= nd.hi[0] && nd.lo[1] <= y && y <= nd.hi[1] && nd.lo[2] <= z &&
-          z <= nd.hi[2]))
-      continue;
-    if (nd.left < 0) {
-      hit = -nd.left - 1;
+    const int ref = stack[--sp];
+    if (ref < 0) {  // a containing leaf: the first in pre-order
+      hit = -ref - 1;
       break;
     }
-    if (sp + 2 > kBvhMaxDepth) break;  // depth is bounded by the build
-    stack[sp++] = nd.right;
-    stack[sp++] = nd.left;
+    const WideNode* w = ref < ntop ? top + ref : wide + ref;
+    float4 b[12];  // lo x, lo y, lo z, hi x, hi y, hi z: two float4 each
+    int4 ch[2];
+    if (ref < ntop) {
+#pragma unroll
+      for (int u = 0; u < 12; ++u) b[u] = reinterpret_cast<const float4*>(w)[u];
+      ch[0] = reinterpret_cast<const int4*>(w->child)[0];
+      ch[1] = reinterpret_cast<const int4*>(w->child)[1];
+    } else {
+#pragma unroll
+      for (int u = 0; u < 12; ++u) b[u] = __ldg(reinterpret_cast<const float4*>(w) + u);
+      ch[0] = __ldg(reinterpret_cast<const int4*>(w->child));
+      ch[1] = __ldg(reinterpret_cast<const int4*>(w->child) + 1);
+    }
+    const float* lo = reinterpret_cast<const float*>(b);
+    const float* hi = lo + 24;
+    const int* child = reinterpret_cast<const int*>(ch);
+#pragma unroll
+    for (int c = kWide - 1; c >= 0; --c) {
+      const bool in = lo[c] <= x && x <= hi[c] && lo[8 + c] <= y && y <= hi[8 + c] &&
+                      lo[16 + c] <= z && z <= hi[16 + c];
+      if (in && sp < kLocStack) stack[sp++] = child[c];
+    }
   }
   out[i] = hit;
 }
@@ -392,8 +431,8 @@ cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const 
                            cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  project_rows<<<grid, 128, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr,
-                                     nullptr, 0.0f, 0);
+  project_rows<false><<<grid, 128, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride,
+                                            nullptr, nullptr, 0.0f, 0);
   return cudaGetLastError();
 }
 
@@ -403,8 +442,8 @@ cudaError_t launch_project_bf16(const float* x, int64_t n, int d, int xstride, c
   if (n == 0) return cudaSuccess;
   if (ld16 < k || ld16 > ((k + kPrCols - 1) / kPrCols) * kPrCols) return cudaErrorInvalidValue;
   dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  project_rows<<<grid, 128, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr,
-                                     reinterpret_cast<__nv_bfloat16*>(out16), s16, ld16);
+  project_rows<true><<<grid, 128, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr,
+                                           reinterpret_cast<__nv_bfloat16*>(out16), s16, ld16);
   return cudaGetLastError();
 }
 
@@ -412,8 +451,8 @@ cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, in
                                const float* mean, const float* V, int vstride, int k, float* out,
                                int ostride, cudaStream_t st) {
   dim3 grid((unsigned)((cap + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  project_rows<<<grid, 128, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride, n_dev,
-                                     nullptr, 0.0f, 0);
+  project_rows<false><<<grid, 128, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride,
+                                            n_dev, nullptr, 0.0f, 0);
   return cudaGetLastError();
 }
 
@@ -450,16 +489,16 @@ cudaError_t launch_dequant(const void* il, const float* scale8, int precision, i
 
 // 64 points per block: enough blocks to spread a batch of a few thousand
 // points over every SM (each block copies the top of the tree once).
-cudaError_t launch_locate(const BvhNode* nodes, int n_nodes, const float* pts, int64_t n, int stride,
+cudaError_t launch_locate(const WideNode* wide, int n_wide, const float* pts, int64_t n, int stride,
                           int32_t* out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  locate_points<<<(unsigned)((n + 63) / 64), 64, 0, st>>>(nodes, n_nodes, pts, n, stride, out, nullptr);
+  locate_points<<<(unsigned)((n + 63) / 64), 64, 0, st>>>(wide, n_wide, pts, n, stride, out, nullptr);
   return cudaGetLastError();
 }
 
-cudaError_t launch_locate_dyn(const BvhNode* nodes, int n_nodes, const float* pts, int64_t cap,
+cudaError_t launch_locate_dyn(const WideNode* wide, int n_wide, const float* pts, int64_t cap,
                               const int* n_dev, int stride, int32_t* out, cudaStream_t st) {
-  locate_points<<<(unsigned)((cap + 63) / 64), 64, 0, st>>>(nodes, n_nodes, pts, cap, stride, out, n_dev);
+  locate_points<<<(unsigned)((cap + 63) / 64), 64, 0, st>>>(wide, n_wide, pts, cap, stride, out, n_dev);
   return cudaGetLastError();
 }
 

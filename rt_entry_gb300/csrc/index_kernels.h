@@ -19,6 +19,21 @@ static_assert(sizeof(BvhNode) == 32, "BvhNode is 32 bytes");
 
 constexpr int kBvhMaxDepth = 64;
 
+// The kd-tree again, 8 wide: a wide node holds the boxes of the binary
+// descendants three levels below one binary node (or of the leaves met
+// before that), in pre-order.  Point location then needs a third of the
+// dependent node loads.  child[c] >= 0 is a wide node, < 0 the leaf
+// -(child+1); unused slots have empty boxes (lo > hi).  Wide nodes are
+// numbered breadth-first.
+constexpr int kWide = 8;
+struct WideNode {
+  float lo[3][kWide];  // lo[axis][child]
+  float hi[3][kWide];
+  int32_t child[kWide];
+  int32_t pad[kWide];
+};
+static_assert(sizeof(WideNode) == 256, "WideNode is 256 bytes");
+
 cudaError_t launch_mean(const float* x, int64_t n, int d, double* partial, int nblocks,
                         double* mean, cudaStream_t st);
 cudaError_t launch_cov(const float* x, int64_t n, int d, const double* mean, double* partial,
@@ -37,7 +52,7 @@ cudaError_t launch_project_bf16(const float* x, int64_t n, int d, int xstride, c
 cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, int d, int xstride,
                                const float* mean, const float* V, int vstride, int k, float* out,
                                int ostride, cudaStream_t st);
-cudaError_t launch_locate_dyn(const BvhNode* nodes, int n_nodes, const float* pts, int64_t cap,
+cudaError_t launch_locate_dyn(const WideNode* wide, int n_wide, const float* pts, int64_t cap,
                               const int* n_dev, int stride, int32_t* out, cudaStream_t st);
 cudaError_t launch_interleave(const float* src, int64_t n, int d, int C, float* il32, void* il16,
                               uint8_t* il8, float* scale8, float* xyz, cudaStream_t st);
@@ -54,7 +69,7 @@ cudaError_t launch_locate_in_subtree(const BvhNode* nodes, const float* pts, int
                                      const int32_t* cls, const unsigned long long* keys,
                                      const int32_t* start_node, const int32_t* fallback_leaf,
                                      int32_t* out, cudaStream_t st);
-cudaError_t launch_locate(const BvhNode* nodes, int n_nodes, const float* pts, int64_t n, int stride,
+cudaError_t launch_locate(const WideNode* wide, int n_wide, const float* pts, int64_t n, int stride,
                           int32_t* out, cudaStream_t st);
 
 }  // namespace rte

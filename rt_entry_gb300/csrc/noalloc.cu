@@ -95,7 +95,7 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   if (s != RTE_OK) return s;
   const int32_t* h = hits;
   if (params->entry_mode == RTE_ENTRY_KDTREE && !h) {
-    RTE_CUDA(launch_locate(x->d_nodes.p, (int)x->d_nodes.n, projected, nq, x->search_dim, scr->hits, st));
+    RTE_CUDA(launch_locate(x->d_wide.p, (int)x->d_wide.n, projected, nq, x->search_dim, scr->hits, st));
     h = scr->hits;
   }
   // the array keeps the previous call's contents: the counter must restart at 0

@@ -71,7 +71,7 @@ rte_status capture(rte_batcher* b) {
     qp = b->dproj.p;
   }
   if (e == cudaSuccess && b->prm.entry_mode == RTE_ENTRY_KDTREE)
-    e = launch_locate_dyn(x->d_nodes.p, (int)x->d_nodes.n, qp, b->cap, b->dn.p, x->search_dim, b->dhits.p, st);
+    e = launch_locate_dyn(x->d_wide.p, (int)x->d_wide.n, qp, b->cap, b->dn.p, x->search_dim, b->dhits.p, st);
   if (e == cudaSuccess) {
     SearchArgs a{};
     a.base = x->il32.p;
