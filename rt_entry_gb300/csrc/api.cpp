@@ -207,6 +207,31 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
   return RTE_OK;
 }
 
+// A second stream per host thread and device, with a fork and a join event,
+// created on first use and kept for the life of the thread.
+struct SideStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+cudaError_t side_stream(int dev, SideStream** out) {
+  thread_local SideStream sides[64];
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  SideStream& sd = sides[dev];
+  if (!sd.s) {
+    cudaError_t e = cudaStreamCreateWithFlags(&sd.s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sd.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sd.join, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      sd = SideStream{};
+      return e;
+    }
+  }
+  *out = &sd;
+  return cudaSuccess;
+}
+
 // Projection + locate + search on device buffers.
 rte_status run_query_path(rte_index* x, const float* d_queries, bool already_projected,
                           const int32_t* d_hits_in, int64_t nq, const rte_search_params* prm,
@@ -243,17 +268,28 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
     hits = hitsb.as<int32_t>();
   }
   if (prm->entry_mode == RTE_ENTRY_LEARNED) {
-    // proposed leaf (MLP) first, kd-tree leaf second
+    // proposed leaf (MLP) first, kd-tree leaf second; when the model runs
+    // here, the kd-tree location runs beside it on this thread's side stream
     RTE_CUDA(hits2b.alloc((size_t)nq * 4, st));
-    RTE_CUDA(launch_locate(x->d_wide.p, (int)x->d_wide.n, qp, nq, x->search_dim, hits2b.as<int32_t>(), st));
     hits2 = hits2b.as<int32_t>();
+    SideStream* sd = nullptr;
+    const bool fork = !hits && side_stream(x->device, &sd) == cudaSuccess;
+    if (fork) {
+      RTE_CUDA(cudaEventRecord(sd->fork, st));
+      RTE_CUDA(cudaStreamWaitEvent(sd->s, sd->fork, 0));
+    }
+    RTE_CUDA(launch_locate(x->d_wide.p, (int)x->d_wide.n, qp, nq, x->search_dim,
+                           hits2b.as<int32_t>(), fork ? sd->s : st));
+    if (fork) RTE_CUDA(cudaEventRecord(sd->join, sd->s));
+    rte_status ls = RTE_OK;
     if (!hits) {
       RTE_CUDA(hitsb.alloc((size_t)nq * 4, st));
-      rte_status ls = learned_leaves(x, qp, nq, hitsb.as<int32_t>(), st,
-                                     xb.p ? xb.as<uint16_t>() : nullptr);
-      if (ls != RTE_OK) return ls;
+      ls = learned_leaves(x, qp, nq, hitsb.as<int32_t>(), st, xb.p ? xb.as<uint16_t>() : nullptr);
       hits = hitsb.as<int32_t>();
     }
+    // join before anything returns: the buffers are freed in stream order on st
+    if (fork) RTE_CUDA(cudaStreamWaitEvent(st, sd->join, 0));
+    if (ls != RTE_OK) return ls;
   }
   RTE_CUDA(work.alloc(4, st));
   RTE_CUDA(cudaMemsetAsync(work.p, 0, 4, st));
@@ -439,7 +475,7 @@ rte_status rte_build_kdtree(rte_index* x, int leaf_size, float expand_ratio) {
   RTE_CUDA(x->d_nodes.alloc(t.nodes.size()));
   RTE_CUDA(cudaMemcpy(x->d_nodes.p, t.nodes.data(), x->d_nodes.bytes(), cudaMemcpyHostToDevice));
   std::vector<WideNode> wide;
-  kd_wide(t, wide);
+  kd_wide(t, wide, &x->wide_of);
   RTE_CUDA(x->d_wide.alloc(wide.size()));
   RTE_CUDA(cudaMemcpy(x->d_wide.p, wide.data(), x->d_wide.bytes(), cudaMemcpyHostToDevice));
   RTE_CUDA(x->d_pids.alloc(t.pids.size()));

@@ -196,7 +196,7 @@ bool kd_build(const float* xyz, int64_t n, int cap, KdTree& out, std::string& er
   return true;
 }
 
-void kd_wide(const KdTree& t, std::vector<WideNode>& out) {
+void kd_wide(const KdTree& t, std::vector<WideNode>& out, std::vector<int32_t>* wide_of) {
   out.clear();
   std::vector<int> start{0};  // binary node that each wide node expands, breadth-first
   std::vector<int> kids;
@@ -243,6 +243,10 @@ void kd_wide(const KdTree& t, std::vector<WideNode>& out) {
       }
     }
     out.push_back(w);
+  }
+  if (wide_of) {
+    wide_of->assign(t.nodes.size(), -1);
+    for (size_t i = 0; i < start.size(); ++i) (*wide_of)[start[i]] = (int32_t)i;
   }
 }
 

@@ -25,7 +25,9 @@ struct KdTree {
 
 // The 8-wide copy of the tree for point location (index_kernels.h), built
 // from the expanded node bounds (call after kd_expand).
-void kd_wide(const KdTree& t, std::vector<WideNode>& out);
+// wide_of (optional): for every binary node that starts a wide node, that
+// wide node's index; -1 elsewhere.
+void kd_wide(const KdTree& t, std::vector<WideNode>& out, std::vector<int32_t>* wide_of = nullptr);
 
 // Returns false (with err) when a split leaves one side empty (the
 // reference exits the process there, kdtree.cpp:182-185).

@@ -107,6 +107,9 @@ struct Mlp {
   int real_classes = 0;
   int depth = 0;
   DevBuf<int32_t> class_node, class_leaf0;
+  // when every class starts a wide node (or is a leaf): its reference in the
+  // 8-wide tree (>= 0 wide node, < 0 the leaf -(ref+1)); empty otherwise
+  DevBuf<int32_t> class_wide;
 };
 
 }  // namespace rte
@@ -139,6 +142,7 @@ struct rte_index {
   float expand_ratio = 0.f;
   rte::DevBuf<rte::BvhNode> d_nodes;
   rte::DevBuf<rte::WideNode> d_wide;  // 8-wide copy for point location
+  std::vector<int32_t> wide_of;       // binary node -> wide node that it starts, or -1
   rte::DevBuf<int32_t> d_pids;
   // learned entry
   rte::Mlp mlp;

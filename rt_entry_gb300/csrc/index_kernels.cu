@@ -289,6 +289,35 @@ __global__ void dequant_rows(const void* __restrict__ il, const float* __restric
 constexpr int kTopWide = 73;
 constexpr int kLocStack = 64;
 
+// One wide-tree step shared by the locate kernels: the containing children of
+// wide node w pushed last-first onto the stack.
+__device__ __forceinline__ void push_containing(const WideNode* w, bool shared_copy, float x, float y,
+                                                float z, int* stack, int& sp) {
+  float4 b[12];  // lo x, lo y, lo z, hi x, hi y, hi z: two float4 each
+  int4 ch[2];
+  if (shared_copy) {
+#pragma unroll
+    for (int u = 0; u < 12; ++u) b[u] = reinterpret_cast<const float4*>(w)[u];
+    ch[0] = reinterpret_cast<const int4*>(w->child)[0];
+    ch[1] = reinterpret_cast<const int4*>(w->child)[1];
+  } else {
+#pragma unroll
+    for (int u = 0; u < 12; ++u) b[u] = __ldg(reinterpret_cast<const float4*>(w) + u);
+    ch[0] = __ldg(reinterpret_cast<const int4*>(w->child));
+    ch[1] = __ldg(reinterpret_cast<const int4*>(w->child) + 1);
+  }
+  const float* lo = reinterpret_cast<const float*>(b);
+  const float* hi = lo + 24;
+  const int* child = reinterpret_cast<const int*>(ch);
+#pragma unroll
+  for (int c = kWide - 1; c >= 0; --c) {
+    const bool in = lo[c] <= x && x <= hi[c] && lo[8 + c] <= y && y <= hi[8 + c] && lo[16 + c] <= z &&
+                    z <= hi[16 + c];
+    if (in && sp < kLocStack) stack[sp++] = child[c];
+  }
+}
+
+
 __global__ void locate_points(const WideNode* __restrict__ wide, int n_wide,
                               const float* __restrict__ pts, int64_t n, int stride,
                               int32_t* __restrict__ out, const int* __restrict__ n_dev) {
@@ -315,29 +344,35 @@ __global__ void locate_points(const WideNode* __restrict__ wide, int n_wide,
       hit = -ref - 1;
       break;
     }
-    const WideNode* w = ref < ntop ? top + ref : wide + ref;
-    float4 b[12];  // lo x, lo y, lo z, hi x, hi y, hi z: two float4 each
-    int4 ch[2];
-    if (ref < ntop) {
-#pragma unroll
-      for (int u = 0; u < 12; ++u) b[u] = reinterpret_cast<const float4*>(w)[u];
-      ch[0] = reinterpret_cast<const int4*>(w->child)[0];
-      ch[1] = reinterpret_cast<const int4*>(w->child)[1];
-    } else {
-#pragma unroll
-      for (int u = 0; u < 12; ++u) b[u] = __ldg(reinterpret_cast<const float4*>(w) + u);
-      ch[0] = __ldg(reinterpret_cast<const int4*>(w->child));
-      ch[1] = __ldg(reinterpret_cast<const int4*>(w->child) + 1);
+    push_containing(ref < ntop ? top + ref : wide + ref, ref < ntop, x, y, z, stack, sp);
+  }
+  out[i] = hit;
+}
+
+// Point location inside the predicted subtree, on the 8-wide tree: the same
+// pre-order search from the subtree's wide node; the subtree's first leaf
+// when none of its leaves contains the point.
+__global__ void locate_in_subtree_wide(const WideNode* __restrict__ wide,
+                                       const float* __restrict__ pts, int64_t n, int stride,
+                                       const unsigned long long* __restrict__ keys,
+                                       const int32_t* __restrict__ start_ref,
+                                       const int32_t* __restrict__ fallback_leaf,
+                                       int32_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = 0x7fffffff - (int)(keys[i] & 0xffffffffu);
+  const float x = pts[i * stride + 0], y = pts[i * stride + 1], z = pts[i * stride + 2];
+  int stack[kLocStack];
+  int sp = 0;
+  stack[sp++] = start_ref[c];
+  int32_t hit = fallback_leaf[c];
+  while (sp > 0) {
+    const int ref = stack[--sp];
+    if (ref < 0) {
+      hit = -ref - 1;
+      break;
     }
-    const float* lo = reinterpret_cast<const float*>(b);
-    const float* hi = lo + 24;
-    const int* child = reinterpret_cast<const int*>(ch);
-#pragma unroll
-    for (int c = kWide - 1; c >= 0; --c) {
-      const bool in = lo[c] <= x && x <= hi[c] && lo[8 + c] <= y && y <= hi[8 + c] &&
-                      lo[16 + c] <= z && z <= hi[16 + c];
-      if (in && sp < kLocStack) stack[sp++] = child[c];
-    }
+    push_containing(wide + ref, false, x, y, z, stack, sp);
   }
   out[i] = hit;
 }
@@ -489,6 +524,16 @@ cudaError_t launch_dequant(const void* il, const float* scale8, int precision, i
 
 // 64 points per block: enough blocks to spread a batch of a few thousand
 // points over every SM (each block copies the top of the tree once).
+cudaError_t launch_locate_in_subtree_wide(const WideNode* wide, const float* pts, int64_t n,
+                                          int stride, const unsigned long long* keys,
+                                          const int32_t* start_ref, const int32_t* fallback_leaf,
+                                          int32_t* out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  locate_in_subtree_wide<<<(unsigned)((n + 63) / 64), 64, 0, st>>>(wide, pts, n, stride, keys,
+                                                                     start_ref, fallback_leaf, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_locate(const WideNode* wide, int n_wide, const float* pts, int64_t n, int stride,
                           int32_t* out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;

@@ -69,6 +69,12 @@ cudaError_t launch_locate_in_subtree(const BvhNode* nodes, const float* pts, int
                                      const int32_t* cls, const unsigned long long* keys,
                                      const int32_t* start_node, const int32_t* fallback_leaf,
                                      int32_t* out, cudaStream_t st);
+// launch_locate_in_subtree on the 8-wide tree: the class of point i, decoded
+// from keys[i], starts at start_ref[class] (a wide node, or a leaf).
+cudaError_t launch_locate_in_subtree_wide(const WideNode* wide, const float* pts, int64_t n,
+                                          int stride, const unsigned long long* keys,
+                                          const int32_t* start_ref, const int32_t* fallback_leaf,
+                                          int32_t* out, cudaStream_t st);
 cudaError_t launch_locate(const WideNode* wide, int n_wide, const float* pts, int64_t n, int stride,
                           int32_t* out, cudaStream_t st);
 

@@ -305,9 +305,15 @@ rte_status learned_leaves(const rte_index* x, const float* d_proj, int64_t nq, i
   if (s != RTE_OK) return s;
   // the model picks the subtree (decoded from its argmax key), the kd-tree
   // picks the leaf inside it
-  RTE_CUDA(launch_locate_in_subtree(x->d_nodes.p, d_proj, nq, x->search_dim, nullptr,
-                                    keys.as<unsigned long long>(), m.class_node.p, m.class_leaf0.p,
-                                    d_leaf, st));
+  if (m.class_wide.p) {
+    RTE_CUDA(launch_locate_in_subtree_wide(x->d_wide.p, d_proj, nq, x->search_dim,
+                                           keys.as<unsigned long long>(), m.class_wide.p,
+                                           m.class_leaf0.p, d_leaf, st));
+  } else {
+    RTE_CUDA(launch_locate_in_subtree(x->d_nodes.p, d_proj, nq, x->search_dim, nullptr,
+                                      keys.as<unsigned long long>(), m.class_node.p,
+                                      m.class_leaf0.p, d_leaf, st));
+  }
   return RTE_OK;
 }
 
@@ -499,6 +505,20 @@ extern "C" rte_status rte_learned_train(rte_index* x, const float* train_queries
   RTE_CUDA(m.class_leaf0.alloc(C));
   RTE_CUDA(cudaMemcpy(m.class_node.p, class_node.data(), C * 4, cudaMemcpyHostToDevice));
   RTE_CUDA(cudaMemcpy(m.class_leaf0.p, class_leaf0.data(), C * 4, cudaMemcpyHostToDevice));
+  {
+    // classes three binary levels apart start wide nodes: locate on the 8-wide tree
+    std::vector<int32_t> ref(C);
+    bool all = x->wide_of.size() == x->kd.nodes.size();
+    for (int64_t c = 0; c < C && all; ++c) {
+      const BvhNode& nd = x->kd.nodes[class_node[c]];
+      ref[c] = nd.left < 0 ? nd.left : x->wide_of[class_node[c]];
+      if (nd.left >= 0 && ref[c] < 0) all = false;
+    }
+    if (all) {
+      RTE_CUDA(m.class_wide.alloc(C));
+      RTE_CUDA(cudaMemcpy(m.class_wide.p, ref.data(), C * 4, cudaMemcpyHostToDevice));
+    }
+  }
   // training accuracy (of the class) on the first batch of the last permutation
   {
     DevBuf<int32_t> pred;
