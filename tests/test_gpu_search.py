@@ -77,6 +77,8 @@ SWEEP = [
     (32, False, 32, 16, 1, 512, 3, 0, 100),
     (128, False, 32, 16, 2, 1024, 3, 1, 100),
     (64, True, 32, 16, 1, 32, 4, 1, 5),
+    (960, False, 64, 64, 1, 512, 3, 1, 100),    # 960 dims: 30 chunks of 32 per row
+    (960, False, 32, 16, 2, 1024, 3, 0, 60),
 ]
 
 
@@ -250,6 +252,26 @@ def test_bf16_tensor_core_distances_on_real_valued_data(lib, orc, cuda, d):
     rec_b = ds.recall_at(ids2, gt, 10)
     rec_f = ds.recall_at(fp32_ids, gt, 10)
     assert rec_b >= rec_f - 0.01, (rec_b, rec_f)
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_high_dim_precisions_match_oracle(lib, orc, cuda, prec):
+    """960 dims (30 chunks): the BF16 and FP8 paths run the scalar distance
+    code there, so both are bit-exact against the oracle on the dequantised
+    base, before and after the FP32 rerank, on real-valued data."""
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(2500, 120, 960, False, seed=960 + prec)
+    graph = ds.knn_graph(base, 64)
+    idx = _index(base, graph, 32, 0.2)
+    _, _, pids = idx.kdtree()
+    hits = idx.locate(q)
+    low = idx.search_base_lowp(prec)
+    for rerank in (0, 1):
+        ids, dd = idx.search_projected(q, beam=64, k=64, precision=prec, rerank=rerank)
+        oids, od = orc.search(low, q, graph, L=64, k=64, leaf_pids=pids, hits=hits,
+                              rerank_base=base if rerank else None)
+        assert np.array_equal(ids, oids), (rerank, f"{(ids != oids).any(1).sum()} queries differ")
+        assert np.array_equal(dd, od)
 
 
 def test_parameter_errors(lib, cuda):
