@@ -59,7 +59,9 @@ typedef struct {
   int bloom_words;   /* visited-set filter size in 32-bit words (SIZE, default 512)   */
   int bloom_hashes;  /* hash functions (num_hash, default 3)                          */
   int precision;     /* rte_precision of candidate distances                          */
-  int rerank;        /* 1: exact FP32 rerank of the final beam (graph_helper.cu:146)  */
+  int rerank;        /* 1: exact FP32 rerank of the final beam in the searched space;
+                        2: exact FP32 rerank of the final beam against the original
+                           (pre-PCA) rows, rte_search only (graph_helper.cu:146-213) */
   int entry_mode;    /* rte_entry_mode                                                */
   int warps_per_block; /* 0 = automatic                                                */
 } rte_search_params;

@@ -95,6 +95,8 @@ def lib():
         L.orc_search_rerank.argtypes = [P, P, i64, i32, P, i64, P, i32, P, i32, P, P, i32, i32,
                                         i32, i32, i32, i32, i32, P, P, P, i32]
         L.orc_search_rerank.restype = i32
+        L.orc_rerank_full.argtypes = [P, i64, i32, P, i64, P, i32, i32, P, P, i32]
+        L.orc_rerank_full.restype = i32
         L.orc_l2_ref.argtypes = [P, P, i32]
         L.orc_l2_ref.restype = f32
         L.orc_kdtree_build.argtypes = [P, i64, i32, i64, P, P, ctypes.POINTER(i64)]
@@ -115,6 +117,23 @@ def _p(a):
 
 def _c(a, dt):
     return np.ascontiguousarray(a, dtype=dt)
+
+
+def rerank_full(base, queries, pool, k, n_threads=0):
+    """Exact FP32 rerank of pools [nq, L] against the original rows -> the
+    first k (ids, dists) of the ascending bitonic sort."""
+    base = _c(base, np.float32)
+    queries = _c(queries, np.float32)
+    pool = _c(pool, np.int32)
+    np_, dim = base.shape
+    nq, L = pool.shape
+    ids = np.empty((nq, k), np.int32)
+    dists = np.empty((nq, k), np.float32)
+    rc = lib().orc_rerank_full(_p(base), np_, dim, _p(queries), nq, _p(pool), L, k, _p(ids),
+                               _p(dists), n_threads)
+    if rc != 0:
+        raise ValueError("orc_rerank_full rejected its arguments")
+    return ids, dists
 
 
 def search(base, queries, graph, *, L, k, search_width=1, max_iter=100, bloom_words=512,

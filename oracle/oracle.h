@@ -65,6 +65,13 @@ int orc_search_rerank(const float* base, const float* rerank_base, int64_t np, i
  * per-lane FMA chain over chunks, then the shfl_down tree 16,8,4,2,1. */
 float orc_l2_ref(const float* p, const float* q, int d);
 
+/* Exact FP32 rerank of pools [nq x L] (ids, visited marks allowed) against
+ * the original rows base [np x dim] and queries [nq x dim]: the first k of
+ * the ascending bitonic sort.  graph_helper.cu:146-213. */
+int orc_rerank_full(const float* base, int64_t np, int dim, const float* queries, int64_t nq,
+                    const int32_t* pool, int L, int k, int32_t* out_ids, float* out_dists,
+                    int n_threads);
+
 /* kd-tree build over 3-d points (kdtree.cpp:4-196).  Outputs leaves in the
  * reference's DFS order: tight boxes [n_leaves x 6] (minX,minY,minZ,maxX,maxY,maxZ)
  * and leaf pids [n_leaves x leaf_cap] padded with np.  The caller passes

@@ -385,3 +385,46 @@ extern "C" int orc_search_rerank(const float* base, const float* rerank_base, in
   (void)n_threads;
   return 0;
 }
+
+// Exact rerank of final pools against the original vectors: the GPU form of
+// the reference's host-side REORDER (parallel_reorder, graph_helper.cu:146-213:
+// FP32 L2 over the original rows of the L pool ids, sorted by distance, the
+// first topk kept).  Distances follow rule H4 (orc_l2_ref); ids >= np get
+// the MAX sentinel.  The sort is the ascending bitonic network over L slots
+// (the reference's std::sort leaves ties unordered; this fixes them: rule H8).
+extern "C" int orc_rerank_full(const float* base, int64_t np, int dim, const float* queries,
+                               int64_t nq, const int32_t* pool, int L, int k, int32_t* out_ids,
+                               float* out_dists, int n_threads) {
+  if (!base || !queries || !pool || !out_ids || L <= 0 || (L & (L - 1)) || k <= 0 || k > L)
+    return -1;
+#ifdef _OPENMP
+  if (n_threads <= 0) n_threads = omp_get_num_procs();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(n_threads)
+#endif
+  for (int64_t qi = 0; qi < nq; ++qi) {
+    std::vector<Pair> na(L);
+    for (int i = 0; i < L; ++i) {
+      int id = pool[qi * L + i];
+      id = id < 0 ? -id : id;
+      na[i].id = id;
+      na[i].d = id < np ? orc_l2_ref(base + (int64_t)id * dim, queries + qi * dim, dim) : ORC_MAX_DIST;
+    }
+    for (int step = 1; step <= L / 2; step *= 2)
+      for (int sub = step; sub >= 1; sub /= 2)
+        for (int i = 0; i < L / 2; ++i) {
+          int a = (i / sub) * 2 * sub + (i & (sub - 1));
+          int b = a + sub;
+          if (((i / step) & 1) == 0) {
+            if (na[a].d > na[b].d) cswap(na[a], na[b]);
+          } else {
+            if (na[a].d < na[b].d) cswap(na[a], na[b]);
+          }
+        }
+    for (int i = 0; i < k; ++i) {
+      out_ids[qi * k + i] = na[i].id;
+      if (out_dists) out_dists[qi * k + i] = na[i].d;
+    }
+  }
+  (void)n_threads;
+  return 0;
+}

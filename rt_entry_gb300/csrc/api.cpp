@@ -20,6 +20,7 @@
 #include "index_impl.h"
 #include "index_kernels.h"
 #include "io.h"
+#include "rerank_full.h"
 #include "search_dispatch.h"
 
 using namespace rte;
@@ -174,6 +175,7 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
     return fail(RTE_EINVAL, "bloom_words must be a power of two in [32, 16384]");
   if (prm->bloom_hashes < 1 || prm->bloom_hashes > 10) return fail(RTE_EINVAL, "bloom_hashes must be in [1, 10]");
   if (prm->precision < 0 || prm->precision > 2) return fail(RTE_EINVAL, "precision must be 0, 1 or 2");
+  if (prm->rerank < 0 || prm->rerank > 2) return fail(RTE_EINVAL, "rerank must be 0, 1 or 2");
   if (prm->entry_mode < RTE_ENTRY_RANDOM || prm->entry_mode > RTE_ENTRY_LEARNED)
     return fail(RTE_EINVAL, "entry_mode must be RTE_ENTRY_RANDOM, _KDTREE or _LEARNED");
   if (prm->entry_mode == RTE_ENTRY_LEARNED && !x->mlp.trained)
@@ -240,6 +242,11 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   rte_status s = plan_search(x, prm, nq, pl);
   if (s != RTE_OK) return s;
   if (nq == 0) return RTE_OK;
+  // rerank 2: the search returns its whole pool, which is reranked against
+  // the original rows and queries (graph_helper.cu:146-213)
+  const bool full_rerank = prm->rerank == 2;
+  if (full_rerank && already_projected)
+    return fail(RTE_EINVAL, "rerank 2 needs the original queries: use rte_search");
   const float* qp = d_queries;
   AsyncBuf proj, hitsb, work, xb;
   // learned entries without caller hits: the projection also writes the
@@ -293,6 +300,8 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   }
   RTE_CUDA(work.alloc(4, st));
   RTE_CUDA(cudaMemsetAsync(work.p, 0, 4, st));
+  AsyncBuf poolb;
+  if (full_rerank) RTE_CUDA(poolb.alloc((size_t)nq * pl.L * 4, st));
   SearchArgs a{};
   a.base = x->il32.p;
   a.base_bf16 = x->il16.p;
@@ -304,8 +313,8 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   a.leaf_pids = x->has_kdtree ? x->d_pids.p : nullptr;
   a.hits = hits;
   a.hits2 = hits2;
-  a.out_ids = d_ids;
-  a.out_dists = d_dists;
+  a.out_ids = full_rerank ? poolb.as<int32_t>() : d_ids;
+  a.out_dists = full_rerank ? nullptr : d_dists;
   a.counters = d_counters;
   a.work = work.as<unsigned int>();
   a.np = (int)x->np;
@@ -314,15 +323,18 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   a.nq = (int)nq;
   a.R = x->degree;
   a.W = prm->search_width;
-  a.k = pl.k;
+  a.k = full_rerank ? pl.L : pl.k;
   a.max_iter = prm->max_iter;
   a.bloom_words = prm->bloom_words;
   a.bloom_hashes = prm->bloom_hashes;
   a.leaf_cap = x->has_kdtree ? x->kd.cap : 1;
   a.entry_mode = prm->entry_mode;
-  a.rerank = prm->rerank;
+  a.rerank = full_rerank ? 0 : prm->rerank;
   a.n_leaves = x->has_kdtree ? (int)x->kd.n_leaves : 1;
   RTE_CUDA(launch_search(a, x->C, pl.NL, pl.NB, pl.prec, pl.wpb, pl.grid, pl.smem, st));
+  if (full_rerank)
+    RTE_CUDA(launch_rerank_full(x->raw.p, x->np, x->dim, d_queries, x->dim, poolb.as<int32_t>(),
+                                (int)nq, pl.L, pl.k, d_ids, d_dists, x->num_sms, st));
   return RTE_OK;
 }
 

@@ -90,6 +90,8 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   size_t smem;
   rte_status s = search_plan(x, params, nq, &L, &k, &NL, &NB, &wpb, &grid, &smem);
   if (s != RTE_OK) return s;
+  if (params->rerank == 2)
+    return fail(RTE_EINVAL, "rerank 2 needs the original queries: use rte_search");
   NoallocScratch* scr = nullptr;
   s = scratch_for_device(x->device, &scr);
   if (s != RTE_OK) return s;

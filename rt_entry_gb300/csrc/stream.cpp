@@ -120,6 +120,7 @@ extern "C" rte_status rte_batcher_create(rte_index* x, int64_t max_nq,
   if (max_nq <= 0 || max_nq >= INT32_MAX) return fail(RTE_EINVAL, "max_nq must be in [1, 2^31)");
   if (params->entry_mode == RTE_ENTRY_LEARNED)
     return fail(RTE_EINVAL, "the batcher serves random and kd-tree entries");
+  if (params->rerank == 2) return fail(RTE_EINVAL, "the batcher does not rerank against the original rows");
   DeviceGuard guard(x->device);
   auto* b = new rte_batcher();
   b->idx = x;

@@ -274,6 +274,33 @@ def test_high_dim_precisions_match_oracle(lib, orc, cuda, prec):
         assert np.array_equal(dd, od)
 
 
+@pytest.mark.parametrize("L", [16, 64])
+def test_truncated_pca_search_with_full_rerank(lib, orc, cuda, L):
+    """Search in 48 of 128 PCA dims, then rerank the final pool exactly
+    against the original rows (rerank 2, the reference's REORDER): bit-exact
+    against the oracle's search in the projected space followed by its
+    full-dimension rerank, and recall no worse than without the rerank."""
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(3000, 150, 128, False, seed=55 + L)
+    graph = ds.knn_graph(base, 64)
+    idx = r.Index.from_arrays(base, graph).build_pca(48).build_kdtree(32, 0.2)
+    assert idx.info.search_dim == 48
+    qp = idx.project(q)
+    _, _, pids = idx.kdtree()
+    hits = idx.locate(qp)
+    ids, dd = idx.search(q, beam=L, k=10, rerank=2)
+    pool, _ = orc.search(idx.search_base(), qp, graph, L=L, k=L, leaf_pids=pids, hits=hits)
+    oids, od = orc.rerank_full(base, q, pool, 10)
+    assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
+    assert np.array_equal(dd, od)
+    gt = ds.ground_truth(base, q, 10)
+    ids0, _ = idx.search(q, beam=L, k=10)
+    assert ds.recall_at(ids, gt, 10) >= ds.recall_at(ids0, gt, 10)
+    with pytest.raises(r.RteError):
+        idx.search_projected(qp, beam=L, k=10, rerank=2)  # needs the original queries
+
+
 def test_parameter_errors(lib, cuda):
     import rt_entry_gb300 as r
     from rt_entry_gb300 import datasets as ds

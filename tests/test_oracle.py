@@ -89,6 +89,28 @@ def test_oracle_l2_matches_fp64_closely(orc):
         assert abs(orc.l2_ref(p, q) - exact) <= 1e-5 * exact
 
 
+def test_oracle_full_rerank(orc):
+    """The full-dimension rerank: the reference's arithmetic on the original
+    rows, ascending, first k; visited marks and padding ids handled."""
+    rng = np.random.default_rng(7)
+    n, dim, nq, L, k = 500, 128, 40, 64, 10
+    base = rng.standard_normal((n, dim)).astype(np.float32)
+    q = rng.standard_normal((nq, dim)).astype(np.float32)
+    pool = np.stack([rng.choice(n, L, replace=False) for _ in range(nq)]).astype(np.int32)
+    pool[:, ::7] *= -1          # visited marks
+    pool[:5, -3:] = n           # padding slots
+    ids, d = orc.rerank_full(base, q, pool, k)
+    for qi in range(nq):
+        cand = np.abs(pool[qi])
+        cand = cand[cand < n]
+        exact = ((base[cand].astype(np.float64) - q[qi]) ** 2).sum(1)
+        want = cand[np.argsort(exact, kind="stable")[:k]]
+        assert set(ids[qi]) == set(want)
+        assert (np.diff(d[qi]) >= 0).all()
+        for j in range(k):
+            assert d[qi, j] == orc.l2_ref(base[ids[qi, j]], q[qi])
+
+
 def test_oracle_recall_on_small_mixture(orc):
     from rt_entry_gb300 import datasets as ds
     mix = ds.mixture_config(1, 32)
