@@ -306,6 +306,16 @@ rte_status rte_gemm_bf16(const uint16_t* A, const uint16_t* B, int M, int N, int
 rte_status rte_gemm_bf16_bias_argmax(const uint16_t* A, const uint16_t* B, const float* bias, int M,
                                      int N, int K, int32_t* cols, void* stream);
 
+/* The exact degree-R kNN graph of base [n x d] (FP32, host or device): row i
+ * lists the R rows j != i nearest to row i by squared L2 distance in FP64,
+ * in (distance, id) order, into graph [n x R] (host or device).  Candidates
+ * come from tensor-core BF16 hi/lo GEMMs; every row is then certified exact
+ * against an error bound, and rows that cannot be certified are redone with
+ * more candidates (RTE_EIO if one still cannot).  The reference loads its
+ * graph from a file (graph.cu:120); no counterpart. */
+rte_status rte_knn_graph(const float* base, int64_t n, int d, int degree, int device, int32_t* graph,
+                         void* stream);
+
 /* Message of the last failure on this thread ("" if none). */
 const char* rte_last_error(void);
 

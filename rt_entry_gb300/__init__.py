@@ -31,7 +31,7 @@ EXPORTS = (
     "rte_get_kdtree", "rte_index_save", "rte_index_load_dir", "rte_index_free", "rte_last_error",
     "rte_kdtree_build_host", "rte_sym_eig_host", "rte_get_search_base_lowp", "rte_gemm_bf16",
     "rte_default_train_params", "rte_learned_train", "rte_learned_predict", "rte_mlp_grad_check",
-    "rte_search_projected_noalloc", "rte_gemm_bf16_bias_argmax", "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
+    "rte_search_projected_noalloc", "rte_gemm_bf16_bias_argmax", "rte_knn_graph", "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
     "rte_batcher_free", "rte_autotune",
 )
 
@@ -123,6 +123,7 @@ def load_library(path: str = LIB_PATH):
         "rte_get_search_base_lowp": ([P, i32, P], i32),
         "rte_gemm_bf16": ([P, P, i32, i32, i32, P, P], i32),
         "rte_gemm_bf16_bias_argmax": ([P, P, P, i32, i32, i32, P, P], i32),
+        "rte_knn_graph": ([P, i64, i32, i32, i32, P, P], i32),
         "rte_default_train_params": ([ctypes.POINTER(TrainParams)], None),
         "rte_learned_train": ([P, P, i64, ctypes.POINTER(TrainParams), ctypes.POINTER(TrainReport)], i32),
         "rte_learned_predict": ([P, P, i64, P, P], i32),
@@ -229,6 +230,19 @@ def bf16_bits(x):
     """FP32 -> BF16 bit patterns (round to nearest even), as uint16."""
     b = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
     return ((b + 0x7FFF + ((b >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def knn_graph(base, degree: int, device: int = 0):
+    """Exact degree-R kNN graph of base [n, d] on the GPU: [n, R] int32, rows
+    in (FP64 distance, id) order, self excluded.  numpy or torch (device) in;
+    numpy out for numpy in, torch for torch."""
+    b = _as(base, np.float32, "float32")
+    n, d = b.shape
+    out = _empty_like_kind(b, (n, degree), np.int32, "int32")
+    pb, kb = _ptr(b)
+    po, ko = _ptr(out)
+    _check(load_library().rte_knn_graph(pb, n, d, degree, device, po, None))
+    return out
 
 
 def gemm_bf16_bias_argmax(a_bits, b_bits, bias):
