@@ -122,8 +122,10 @@ def mixture_config(cfg: int, d: int | None = None) -> Mixture:
 
 def make_config(cfg: int, n: int | None = None, nq: int | None = None, d: int | None = None,
                 with_graph: bool = True, with_gt: bool = True, gt_k: int = 100,
-                device: str | None = None) -> Workload:
-    """Config 1..4 at its published size (or the given n / nq / d)."""
+                device: str | None = None, fast_graph: bool = True) -> Workload:
+    """Config 1..4 at its published size (or the given n / nq / d).  With
+    fast_graph the kNN graph comes from this library's GPU builder (the same
+    exact graph as knn_graph)."""
     sizes = {1: (100_000, 10_000, 32), 2: (1_000_000, 10_000, 64), 3: (1_000_000, 1_000, 64),
              4: (10_000_000, 10_000, 32)}
     n0, nq0, R = sizes[cfg]
@@ -141,7 +143,7 @@ def make_config(cfg: int, n: int | None = None, nq: int | None = None, d: int | 
         q = mix.sample(nq, SEED_QUERY)
     w = Workload(f"config{cfg}", base, q, R, mixture=mix)
     if with_graph:
-        w.graph = knn_graph(base, R, device=device)
+        w.graph = (knn_graph_fast if fast_graph else knn_graph)(base, R, device=device)
     if with_gt:
         w.gt = ground_truth(base, q, min(gt_k, n), device=device)
     return w
@@ -171,6 +173,17 @@ def _sort_by_dist_then_id(d, i):
     """Rows of (dist, id) candidates -> lexicographic order (numpy)."""
     o = np.lexsort((i, d), axis=-1)
     return np.take_along_axis(d, o, -1), np.take_along_axis(i, o, -1)
+
+
+def knn_graph_fast(base: np.ndarray, R: int, device: str | None = None) -> np.ndarray:
+    """The same exact graph as knn_graph, built by this library's GPU builder
+    (rte_knn_graph) when a CUDA device is given, else by knn_graph."""
+    torch, dev = _torch_device(device)
+    if dev is None or dev.type != "cuda":
+        return knn_graph(base, R, device=device)
+    from rt_entry_gb300 import knn_graph as rte_knn_graph
+    return np.asarray(rte_knn_graph(np.ascontiguousarray(base, np.float32), R,
+                                    device=dev.index or 0))
 
 
 def knn_graph(base: np.ndarray, R: int, device: str | None = None, chunk: int = 4096) -> np.ndarray:
