@@ -355,11 +355,8 @@ def main():
         head_ms = timed(p_head, args.steps, args.warmup)
         torch.cuda.nvtx.range_pop()
     head_ids = out_ids.cpu().numpy()
-    total_s = sum(head_ms) / 1000.0
-    if dist:
-        t = torch.tensor([total_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
+    from rt_entry_gb300.replicas import max_over_ranks
+    total_s = max_over_ranks(sum(head_ms) / 1000.0, device=dev)  # the slowest replica
     value = nq * args.steps * world / total_s
     head_recall = ds.recall_at(head_ids, w.gt, K_TOP)
     torch.cuda.nvtx.range_push("rte_timed_plain")
