@@ -446,6 +446,19 @@ def main():
     if rank == 0 and not args.no_stream:
         stream_res = stream_bench(idx, r, ds, torch, stream)
         log(f"stream {stream_res}")
+    # kd-tree entries from several containing leaves (the reference's
+    # disabled multi-hit entry), FP32: informational
+    multi_res = []
+    if rank == 0:
+        for H in (2, 4):
+            for L in (16, 32):
+                p = r.default_params(beam=L, k=K_TOP, max_hits=H)
+                idx.search(qd, params=p, stream=stream, out_ids=out_ids, out_dists=out_d)
+                torch.cuda.synchronize(dev)
+                rec = ds.recall_at(out_ids.cpu().numpy(), w.gt, K_TOP)
+                ms = statistics.median(timed(p, 5, 1))
+                multi_res.append({"max_hits": H, "beam": L, "recall": round(rec, 4), "ms": round(ms, 3)})
+        log(f"multi-leaf {multi_res}")
     trunc_res = None
     if rank == 0:
         trunc_res = truncated_pca_bench(w, r, ds, torch, stream, flush, dev)
@@ -469,6 +482,7 @@ def main():
                               "speedup_of_headline": value / plain_qps},
                "stream": stream_res,
                "truncated_pca": trunc_res,
+               "multi_leaf_kdtree": multi_res or None,
                "roofline": roof_plain,
                "roofline_headline": roof_head,
                "cpu_baseline": cpu,

@@ -64,6 +64,9 @@ typedef struct {
                            (pre-PCA) rows, rte_search only (graph_helper.cu:146-213) */
   int entry_mode;    /* rte_entry_mode                                                */
   int warps_per_block; /* 0 = automatic                                                */
+  int max_hits;      /* kd-tree entries from the first max_hits containing leaves (1..8;
+                        the reference's max_hits, flags.cpp:100, multi-hit entry
+                        entry_helper.cu:5-241); caller hits are then [nq x max_hits]  */
 } rte_search_params;
 
 typedef struct {
@@ -305,6 +308,14 @@ rte_status rte_gemm_bf16(const uint16_t* A, const uint16_t* B, int M, int N, int
  * Host or device pointers; cols [M] int32.  (No reference counterpart.) */
 rte_status rte_gemm_bf16_bias_argmax(const uint16_t* A, const uint16_t* B, const float* bias, int M,
                                      int N, int K, int32_t* cols, void* stream);
+
+/* The first max_hits (1..8) leaves whose expanded boxes contain each
+ * projected query, smallest index first, -1 padded; a query in no box gets
+ * leaf 0 first.  out [nq x max_hits].  Host or device pointers.  The entry
+ * stage of kd-tree search with max_hits > 1 (raytracing.cpp:283-334 with
+ * max_hits, entry_helper.cu:5-241). */
+rte_status rte_locate_multi(rte_index* idx, const float* projected, int64_t nq, int max_hits,
+                            int32_t* out_leaves, void* stream);
 
 /* The exact degree-R kNN graph of base [n x d] (FP32, host or device): row i
  * lists the R rows j != i nearest to row i by squared L2 distance in FP64,

@@ -95,6 +95,11 @@ def lib():
         L.orc_search_rerank.argtypes = [P, P, i64, i32, P, i64, P, i32, P, i32, P, P, i32, i32,
                                         i32, i32, i32, i32, i32, P, P, P, i32]
         L.orc_search_rerank.restype = i32
+        L.orc_search_multi.argtypes = [P, i64, i32, P, i64, P, i32, P, i32, P, i32, i32, i32, i32,
+                                       i32, i32, i32, P, P, P, i32]
+        L.orc_search_multi.restype = i32
+        L.orc_locate_multi.argtypes = [P, i64, P, i64, i32, i32, P, i32]
+        L.orc_locate_multi.restype = None
         L.orc_rerank_full.argtypes = [P, i64, i32, P, i64, P, i32, i32, P, P, i32]
         L.orc_rerank_full.restype = i32
         L.orc_l2_ref.argtypes = [P, P, i32]
@@ -117,6 +122,41 @@ def _p(a):
 
 def _c(a, dt):
     return np.ascontiguousarray(a, dtype=dt)
+
+
+def locate_multi(boxes, qp, H, n_threads=0):
+    """The H smallest-index expanded leaf boxes containing each point
+    ([nq, H], -1 padded)."""
+    boxes = _c(boxes, np.float32)
+    qp = _c(qp, np.float32)
+    out = np.empty((qp.shape[0], H), np.int32)
+    lib().orc_locate_multi(_p(boxes), boxes.shape[0], _p(qp), qp.shape[0], qp.shape[1], H, _p(out),
+                           n_threads)
+    return out
+
+
+def search_multi(base, queries, graph, *, L, k, hits_multi, leaf_pids, search_width=1,
+                 max_iter=100, bloom_words=512, bloom_hashes=3, n_threads=0, with_counters=False):
+    """Kd-tree entries from several leaves per query (hits_multi [nq, H])."""
+    base = _c(base, np.float32)
+    queries = _c(queries, np.float32)
+    graph = _c(graph, np.int32)
+    hm = _c(hits_multi, np.int32)
+    lp = _c(leaf_pids, np.int32)
+    np_, d = base.shape
+    nq = queries.shape[0]
+    ids = np.empty((nq, k), np.int32)
+    dists = np.empty((nq, k), np.float32)
+    cnt = (Counters * max(nq, 1))() if with_counters else None
+    rc = lib().orc_search_multi(_p(base), np_, d, _p(queries), nq, _p(graph), graph.shape[1], _p(lp),
+                                lp.shape[1], _p(hm), hm.shape[1], L, k, search_width, max_iter,
+                                bloom_words, bloom_hashes, _p(ids), _p(dists),
+                                None if cnt is None else ctypes.cast(cnt, ctypes.c_void_p), n_threads)
+    if rc != 0:
+        raise ValueError("orc_search_multi rejected its arguments")
+    if with_counters:
+        return ids, dists, np.frombuffer(cnt, dtype=np.int64).reshape(-1, 4)[:nq].copy()
+    return ids, dists
 
 
 def rerank_full(base, queries, pool, k, n_threads=0):

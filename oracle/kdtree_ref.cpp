@@ -184,6 +184,30 @@ extern "C" void orc_locate(const float* boxes, int64_t n_leaves, const float* qp
   (void)n_threads;
 }
 
+// The first H containing leaves in index order (rule H1 extended to the
+// reference's max_hits > 1); -1 where fewer contain the point; a point in no
+// leaf gets leaf 0 first, as with one leaf.
+extern "C" void orc_locate_multi(const float* boxes, int64_t n_leaves, const float* qp, int64_t nq,
+                                 int stride, int H, int32_t* out_leaves, int n_threads) {
+#ifdef _OPENMP
+  if (n_threads <= 0) n_threads = omp_get_num_procs();
+#pragma omp parallel for schedule(static) num_threads(n_threads)
+#endif
+  for (int64_t q = 0; q < nq; q++) {
+    const float* p = qp + q * stride;
+    int found = 0;
+    for (int64_t i = 0; i < n_leaves && found < H; i++) {
+      const float* b = boxes + 6 * i;
+      if (b[0] <= p[0] && p[0] <= b[3] && b[1] <= p[1] && p[1] <= b[4] && b[2] <= p[2] &&
+          p[2] <= b[5])
+        out_leaves[q * H + found++] = (int32_t)i;
+    }
+    if (found == 0) out_leaves[q * H + found++] = 0;  // a miss enters at leaf 0 (H1)
+    for (; found < H; ++found) out_leaves[q * H + found] = -1;
+  }
+  (void)n_threads;
+}
+
 extern "C" void orc_knn_fp64(const float* base, int64_t np, int d, const float* queries,
                              int64_t nq, int k, int32_t* out_ids, double* out_d2, int n_threads) {
 #ifdef _OPENMP

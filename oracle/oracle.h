@@ -65,6 +65,18 @@ int orc_search_rerank(const float* base, const float* rerank_base, int64_t np, i
  * per-lane FMA chain over chunks, then the shfl_down tree 16,8,4,2,1. */
 float orc_l2_ref(const float* p, const float* q, int d);
 
+/* Entry mode 1 with max_hits leaves per query, hits_multi [nq x max_hits]
+ * (-1 padded): every point of each leaf, max(L, max_hits*leaf_cap) entry
+ * slots.  The reference's disabled multi-hit entry (entry_helper.cu:5-241). */
+int orc_search_multi(const float* base, int64_t np, int d, const float* queries, int64_t nq,
+                     const int32_t* graph, int degree, const int32_t* leaf_pids, int leaf_cap,
+                     const int32_t* hits_multi, int max_hits, int L, int k, int search_width,
+                     int max_iter, int bloom_words, int bloom_hashes, int32_t* out_ids,
+                     float* out_dists, orc_counters* counters, int n_threads);
+/* The first H containing leaves in index order, -1 padded. */
+void orc_locate_multi(const float* boxes, int64_t n_leaves, const float* qp, int64_t nq, int stride,
+                      int H, int32_t* out_leaves, int n_threads);
+
 /* Exact FP32 rerank of pools [nq x L] (ids, visited marks allowed) against
  * the original rows base [np x dim] and queries [nq x dim]: the first k of
  * the ascending bitonic sort.  graph_helper.cu:146-213. */

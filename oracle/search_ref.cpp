@@ -163,6 +163,8 @@ struct SearchArgs {
   const int32_t* leaf_pids;
   int leaf_cap;
   int L, k, W, max_iter, bloom_words, bloom_hashes, entry_mode;
+  int max_hits = 1;                   // entry mode 1: leaves per query
+  const int32_t* hits_multi = nullptr;  // [nq][max_hits] when max_hits > 1, -1 padded
 };
 
 // One query, one "block" of the reference.
@@ -187,7 +189,15 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
   const bool two = A.entry_mode == 2 && hit2 >= 0 && hit2 != hit;
   const int n_first = A.leaf_cap;
   const int n_second = two ? A.leaf_cap : 0;
-  const int n_entries = A.entry_mode == 2 ? std::max(L, n_first + n_second) : L;  // :479
+  // Entry mode 1 with max_hits H > 1 (the reference's disabled multi-hit
+  // entry, entry_helper.cu:5-241): every point of each of the H leaves
+  // (slots h*leaf_cap + j, -1 leaves padded with np), max(L, H*leaf_cap)
+  // entry slots; the pool keeps the best L.
+  const int H = A.entry_mode == 1 ? A.max_hits : 1;
+  const int32_t* hm = H > 1 ? A.hits_multi + qid * H : nullptr;
+  const int n_entries = A.entry_mode == 2 ? std::max(L, n_first + n_second)
+                        : H > 1            ? std::max(L, H * A.leaf_cap)
+                                           : L;  // :479
   const int n_ebatch = (n_entries + B - 1) / B;
   for (int it = 0; it < n_ebatch; ++it) {
     for (int i = 0; i < B; ++i) {
@@ -198,7 +208,11 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
           id = (int)lcg_next(seed[i % 64], (uint32_t)np);
         } else {
           // entry.cu:60-69 (mode 1: the leaf's points, then padding)
-          if (j < n_first)
+          if (H > 1) {
+            const int h = j / A.leaf_cap, s = j - h * A.leaf_cap;
+            const int lf = h < H ? hm[h] : -1;
+            id = lf >= 0 ? A.leaf_pids[(int64_t)lf * A.leaf_cap + s] : np;
+          } else if (j < n_first)
             id = A.leaf_pids[(int64_t)hit * A.leaf_cap + j];
           else if (j < n_first + n_second)
             id = A.leaf_pids[(int64_t)hit2 * A.leaf_cap + (j - n_first)];
@@ -380,6 +394,37 @@ extern "C" int orc_search_rerank(const float* base, const float* rerank_base, in
   for (int64_t qi = 0; qi < nq; ++qi) {
     search_one(A, queries + qi * d, qi, entry_mode != 0 ? hits[qi] : 0,
                entry_mode == 2 ? hits2[qi] : -1, out_ids + qi * k,
+               out_dists ? out_dists + qi * k : nullptr, counters ? counters + qi : nullptr);
+  }
+  (void)n_threads;
+  return 0;
+}
+
+// Entry mode 1 with several leaves per query: hits_multi [nq][max_hits]
+// (-1 padded), the H smallest containing leaf indices (orc_locate_multi).
+extern "C" int orc_search_multi(const float* base, int64_t np, int d, const float* queries,
+                                int64_t nq, const int32_t* graph, int degree,
+                                const int32_t* leaf_pids, int leaf_cap, const int32_t* hits_multi,
+                                int max_hits, int L, int k, int search_width, int max_iter,
+                                int bloom_words, int bloom_hashes, int32_t* out_ids,
+                                float* out_dists, orc_counters* counters, int n_threads) {
+  if (!base || !queries || !graph || !out_ids || !leaf_pids || !hits_multi || leaf_cap <= 0 ||
+      max_hits < 1 || np <= 0 || np >= (int64_t)INT32_MAX || d <= 0 || nq < 0 || degree <= 0 ||
+      (degree & (degree - 1)) || L <= 0 || (L & (L - 1)) || k <= 0 || k > L || search_width <= 0 ||
+      max_iter < 0 || bloom_words <= 0 || (bloom_words & (bloom_words - 1)) || bloom_hashes <= 0 ||
+      bloom_hashes > 10)
+    return -1;
+  SearchArgs A{base, nullptr, np, d, graph, degree, leaf_pids, leaf_cap, L, k, search_width,
+               max_iter, bloom_words, bloom_hashes, 1};
+  A.max_hits = max_hits;
+  A.hits_multi = hits_multi;
+#ifdef _OPENMP
+  if (n_threads <= 0) n_threads = omp_get_num_procs();
+#pragma omp parallel for schedule(dynamic, 4) num_threads(n_threads)
+#endif
+  for (int64_t qi = 0; qi < nq; ++qi) {
+    const int32_t h0 = hits_multi[qi * max_hits];
+    search_one(A, queries + qi * d, qi, h0 >= 0 ? h0 : 0, -1, out_ids + qi * k,
                out_dists ? out_dists + qi * k : nullptr, counters ? counters + qi : nullptr);
   }
   (void)n_threads;

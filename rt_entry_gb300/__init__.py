@@ -31,7 +31,7 @@ EXPORTS = (
     "rte_get_kdtree", "rte_index_save", "rte_index_load_dir", "rte_index_free", "rte_last_error",
     "rte_kdtree_build_host", "rte_sym_eig_host", "rte_get_search_base_lowp", "rte_gemm_bf16",
     "rte_default_train_params", "rte_learned_train", "rte_learned_predict", "rte_mlp_grad_check",
-    "rte_search_projected_noalloc", "rte_gemm_bf16_bias_argmax", "rte_knn_graph", "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
+    "rte_search_projected_noalloc", "rte_gemm_bf16_bias_argmax", "rte_knn_graph", "rte_locate_multi", "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
     "rte_batcher_free", "rte_autotune",
 )
 
@@ -41,7 +41,7 @@ class SearchParams(ctypes.Structure):
                 ("max_iter", ctypes.c_int), ("bloom_words", ctypes.c_int),
                 ("bloom_hashes", ctypes.c_int), ("precision", ctypes.c_int),
                 ("rerank", ctypes.c_int), ("entry_mode", ctypes.c_int),
-                ("warps_per_block", ctypes.c_int)]
+                ("warps_per_block", ctypes.c_int), ("max_hits", ctypes.c_int)]
 
 
 class IndexInfo(ctypes.Structure):
@@ -124,6 +124,7 @@ def load_library(path: str = LIB_PATH):
         "rte_gemm_bf16": ([P, P, i32, i32, i32, P, P], i32),
         "rte_gemm_bf16_bias_argmax": ([P, P, P, i32, i32, i32, P, P], i32),
         "rte_knn_graph": ([P, i64, i32, i32, i32, P, P], i32),
+        "rte_locate_multi": ([P, P, i64, i32, P, P], i32),
         "rte_default_train_params": ([ctypes.POINTER(TrainParams)], None),
         "rte_learned_train": ([P, P, i64, ctypes.POINTER(TrainParams), ctypes.POINTER(TrainReport)], i32),
         "rte_learned_predict": ([P, P, i64, P, P], i32),
@@ -367,12 +368,19 @@ class Index:
         _check(load_library().rte_project(self._h, pq, queries.shape[0], po, _stream_ptr(stream)))
         return out
 
-    def locate(self, projected, stream=None):
+    def locate(self, projected, stream=None, max_hits: int = 1):
+        """Leaf per projected query ([nq]); with max_hits > 1 the first
+        max_hits containing leaves ([nq, max_hits], -1 padded)."""
         projected = _as(projected, np.float32, "float32")
-        out = _empty_like_kind(projected, (projected.shape[0],), np.int32, "int32")
+        shape = (projected.shape[0],) if max_hits == 1 else (projected.shape[0], max_hits)
+        out = _empty_like_kind(projected, shape, np.int32, "int32")
         pp, kp = _ptr(projected)
         po, ko = _ptr(out)
-        _check(load_library().rte_locate(self._h, pp, projected.shape[0], po, _stream_ptr(stream)))
+        if max_hits == 1:
+            _check(load_library().rte_locate(self._h, pp, projected.shape[0], po, _stream_ptr(stream)))
+        else:
+            _check(load_library().rte_locate_multi(self._h, pp, projected.shape[0], max_hits, po,
+                                                   _stream_ptr(stream)))
         return out
 
     def _params(self, params, kw):

@@ -176,6 +176,9 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
   if (prm->bloom_hashes < 1 || prm->bloom_hashes > 10) return fail(RTE_EINVAL, "bloom_hashes must be in [1, 10]");
   if (prm->precision < 0 || prm->precision > 2) return fail(RTE_EINVAL, "precision must be 0, 1 or 2");
   if (prm->rerank < 0 || prm->rerank > 2) return fail(RTE_EINVAL, "rerank must be 0, 1 or 2");
+  if (prm->max_hits < 1 || prm->max_hits > kMaxHits) return fail(RTE_EINVAL, "max_hits must be in [1, 8]");
+  if (prm->max_hits > 1 && prm->entry_mode != RTE_ENTRY_KDTREE)
+    return fail(RTE_EINVAL, "max_hits > 1 needs kd-tree entries");
   if (prm->entry_mode < RTE_ENTRY_RANDOM || prm->entry_mode > RTE_ENTRY_LEARNED)
     return fail(RTE_EINVAL, "entry_mode must be RTE_ENTRY_RANDOM, _KDTREE or _LEARNED");
   if (prm->entry_mode == RTE_ENTRY_LEARNED && !x->mlp.trained)
@@ -270,8 +273,12 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   const int32_t* hits2 = nullptr;
   AsyncBuf hits2b;
   if (prm->entry_mode == RTE_ENTRY_KDTREE && !hits) {
-    RTE_CUDA(hitsb.alloc((size_t)nq * 4, st));
-    RTE_CUDA(launch_locate(x->d_wide.p, (int)x->d_wide.n, qp, nq, x->search_dim, hitsb.as<int32_t>(), st));
+    RTE_CUDA(hitsb.alloc((size_t)nq * prm->max_hits * 4, st));
+    if (prm->max_hits > 1)
+      RTE_CUDA(launch_locate_multi(x->d_wide.p, (int)x->d_wide.n, qp, nq, x->search_dim, prm->max_hits,
+                                   hitsb.as<int32_t>(), st));
+    else
+      RTE_CUDA(launch_locate(x->d_wide.p, (int)x->d_wide.n, qp, nq, x->search_dim, hitsb.as<int32_t>(), st));
     hits = hitsb.as<int32_t>();
   }
   if (prm->entry_mode == RTE_ENTRY_LEARNED) {
@@ -331,6 +338,7 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   a.entry_mode = prm->entry_mode;
   a.rerank = full_rerank ? 0 : prm->rerank;
   a.n_leaves = x->has_kdtree ? (int)x->kd.n_leaves : 1;
+  a.max_hits = prm->max_hits;
   RTE_CUDA(launch_search(a, x->C, pl.NL, pl.NB, pl.prec, pl.wpb, pl.grid, pl.smem, st));
   if (full_rerank)
     RTE_CUDA(launch_rerank_full(x->raw.p, x->np, x->dim, d_queries, x->dim, poolb.as<int32_t>(),
@@ -382,6 +390,7 @@ void rte_default_params(rte_search_params* p) {
   p->rerank = 0;
   p->entry_mode = RTE_ENTRY_KDTREE;
   p->warps_per_block = 0;
+  p->max_hits = 1;
 }
 
 const char* rte_last_error(void) { return g_err.c_str(); }
@@ -561,6 +570,37 @@ rte_status rte_locate(rte_index* x, const float* projected, int64_t nq, int32_t*
   return RTE_OK;
 }
 
+rte_status rte_locate_multi(rte_index* x, const float* projected, int64_t nq, int max_hits,
+                            int32_t* out_leaves, void* stream) {
+  g_err.clear();
+  if (!x || (!projected && nq) || (!out_leaves && nq)) return fail(RTE_EINVAL, "NULL argument");
+  if (nq < 0) return fail(RTE_EINVAL, "nq < 0");
+  if (max_hits < 1 || max_hits > kMaxHits) return fail(RTE_EINVAL, "max_hits must be in [1, 8]");
+  if (!x->has_kdtree) return fail(RTE_ESTATE, "rte_locate_multi before rte_build_kdtree");
+  if (nq == 0) return RTE_OK;
+  DeviceGuard g(x->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool pd = is_device_ptr(projected), od = is_device_ptr(out_leaves);
+  AsyncBuf pb, ob;
+  const float* dp = projected;
+  if (!pd) {
+    RTE_CUDA(pb.alloc((size_t)nq * x->search_dim * 4, st));
+    RTE_CUDA(cudaMemcpyAsync(pb.p, projected, (size_t)nq * x->search_dim * 4, cudaMemcpyHostToDevice, st));
+    dp = pb.as<float>();
+  }
+  int32_t* dout = out_leaves;
+  if (!od) {
+    RTE_CUDA(ob.alloc((size_t)nq * max_hits * 4, st));
+    dout = ob.as<int32_t>();
+  }
+  RTE_CUDA(launch_locate_multi(x->d_wide.p, (int)x->d_wide.n, dp, nq, x->search_dim, max_hits, dout, st));
+  if (!od) {
+    RTE_CUDA(cudaMemcpyAsync(out_leaves, dout, (size_t)nq * max_hits * 4, cudaMemcpyDeviceToHost, st));
+    RTE_CUDA(cudaStreamSynchronize(st));
+  }
+  return RTE_OK;
+}
+
 static rte_status search_common(rte_index* x, const float* q, bool projected, const int32_t* hits,
                                 int64_t nq, const rte_search_params* prm, int32_t* out_ids,
                                 float* out_dists, int64_t* counters, void* stream) {
@@ -589,8 +629,11 @@ static rte_status search_common(rte_index* x, const float* q, bool projected, co
   const int32_t* dh = hits;
   if (hits && !is_device_ptr(hits)) {
     host_io = true;
-    RTE_CUDA(hb.alloc((size_t)nq * 4, st));
-    RTE_CUDA(cudaMemcpyAsync(hb.p, hits, (size_t)nq * 4, cudaMemcpyHostToDevice, st));
+    // [nq x max_hits] for kd-tree entries from several leaves, else [nq]
+    const size_t hbytes = (size_t)nq * 4 *
+                          (prm->entry_mode == RTE_ENTRY_KDTREE && prm->max_hits > 1 ? prm->max_hits : 1);
+    RTE_CUDA(hb.alloc(hbytes, st));
+    RTE_CUDA(cudaMemcpyAsync(hb.p, hits, hbytes, cudaMemcpyHostToDevice, st));
     dh = hb.as<int32_t>();
   }
   int32_t* di = out_ids;

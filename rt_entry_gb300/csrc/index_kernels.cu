@@ -349,6 +349,40 @@ __global__ void locate_points(const WideNode* __restrict__ wide, int n_wide,
   out[i] = hit;
 }
 
+// The first H containing leaves in pre-order (the H smallest indices), -1
+// padded; leaf 0 first when none contains the point.  The same search as
+// locate_points, continued past the first leaf.
+__global__ void locate_points_multi(const WideNode* __restrict__ wide, int n_wide,
+                                    const float* __restrict__ pts, int64_t n, int stride, int H,
+                                    int32_t* __restrict__ out) {
+  __shared__ WideNode top[kTopWide];
+  if ((int64_t)blockIdx.x * blockDim.x >= n) return;
+  const int ntop = min(kTopWide, n_wide);
+  {
+    const float4* src = reinterpret_cast<const float4*>(wide);
+    float4* dst = reinterpret_cast<float4*>(top);
+    for (int i = threadIdx.x; i < 16 * ntop; i += blockDim.x) dst[i] = __ldg(src + i);
+    __syncthreads();
+  }
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float x = pts[i * stride + 0], y = pts[i * stride + 1], z = pts[i * stride + 2];
+  int stack[kLocStack];
+  int sp = 0;
+  stack[sp++] = 0;
+  int found = 0;
+  while (sp > 0 && found < H) {
+    const int ref = stack[--sp];
+    if (ref < 0) {
+      out[i * H + found++] = -ref - 1;
+      continue;
+    }
+    push_containing(ref < ntop ? top + ref : wide + ref, ref < ntop, x, y, z, stack, sp);
+  }
+  if (found == 0) out[i * H + found++] = 0;
+  for (; found < H; ++found) out[i * H + found] = -1;
+}
+
 // Point location inside the predicted subtree, on the 8-wide tree: the same
 // pre-order search from the subtree's wide node; the subtree's first leaf
 // when none of its leaves contains the point.
@@ -531,6 +565,13 @@ cudaError_t launch_locate_in_subtree_wide(const WideNode* wide, const float* pts
   if (n == 0) return cudaSuccess;
   locate_in_subtree_wide<<<(unsigned)((n + 63) / 64), 64, 0, st>>>(wide, pts, n, stride, keys,
                                                                      start_ref, fallback_leaf, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_locate_multi(const WideNode* wide, int n_wide, const float* pts, int64_t n,
+                                int stride, int H, int32_t* out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  locate_points_multi<<<(unsigned)((n + 63) / 64), 64, 0, st>>>(wide, n_wide, pts, n, stride, H, out);
   return cudaGetLastError();
 }
 

@@ -75,6 +75,10 @@ cudaError_t launch_locate_in_subtree_wide(const WideNode* wide, const float* pts
                                           int stride, const unsigned long long* keys,
                                           const int32_t* start_ref, const int32_t* fallback_leaf,
                                           int32_t* out, cudaStream_t st);
+// The first H containing leaves per point ([n][H], -1 padded, leaf 0 first on
+// a miss).
+cudaError_t launch_locate_multi(const WideNode* wide, int n_wide, const float* pts, int64_t n,
+                                int stride, int H, int32_t* out, cudaStream_t st);
 cudaError_t launch_locate(const WideNode* wide, int n_wide, const float* pts, int64_t n, int stride,
                           int32_t* out, cudaStream_t st);
 

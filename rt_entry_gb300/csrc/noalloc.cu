@@ -92,6 +92,7 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   if (s != RTE_OK) return s;
   if (params->rerank == 2)
     return fail(RTE_EINVAL, "rerank 2 needs the original queries: use rte_search");
+  if (params->max_hits > 1) return fail(RTE_EINVAL, "max_hits > 1 needs rte_search");
   NoallocScratch* scr = nullptr;
   s = scratch_for_device(x->device, &scr);
   if (s != RTE_OK) return s;
@@ -131,6 +132,7 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   a.entry_mode = params->entry_mode;
   a.rerank = params->rerank;
   a.n_leaves = x->has_kdtree ? (int)x->kd.n_leaves : 1;
+  a.max_hits = 1;
   RTE_CUDA(launch_search(a, x->C, NL, NB, params->precision, wpb, grid, smem, st));
   return RTE_OK;
 }

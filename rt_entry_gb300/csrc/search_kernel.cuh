@@ -497,7 +497,12 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
   __syncwarp();
 
   // ---- entry phase (graph_search.cuh:479-959) ----
-  int hit = a.entry_mode != 0 ? __ldg(a.hits + q) : 0;
+  // kd-tree entries from several leaves (mode 1, max_hits H > 1, the
+  // reference's multi-hit entry, entry_helper.cu:5-241): every point of each
+  // leaf, leaf h in slots [h*cap, (h+1)*cap), -1 leaves as padding,
+  // max(L, H*cap) entry slots; the pool keeps the best L.
+  const int H = a.entry_mode == 1 ? a.max_hits : 1;
+  int hit = a.entry_mode != 0 ? __ldg(a.hits + (size_t)q * H) : 0;
   if (hit < 0 || hit >= a.n_leaves) hit = 0;
   const int32_t* lp = a.leaf_pids + (size_t)hit * a.leaf_cap;
   // learned entries (mode 2): every point of the proposed leaf, then every
@@ -508,7 +513,9 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
   const int32_t* lp2 = a.leaf_pids + (size_t)(hit2 < 0 ? 0 : hit2) * a.leaf_cap;
   const int n_first = a.leaf_cap;
   const int n_second = hit2 >= 0 ? a.leaf_cap : 0;
-  const int n_entries = a.entry_mode == 2 ? max(L, n_first + n_second) : L;
+  const int n_entries = a.entry_mode == 2 ? max(L, n_first + n_second)
+                        : H > 1            ? max(L, H * a.leaf_cap)
+                                           : L;
   uint32_t seed0 = (uint32_t)q * 64u + (uint32_t)lane;  // reference thread `lane`
   uint32_t seed1 = seed0 + 32u;                           // reference thread `lane + 32`
   const int n_ebatch = (n_entries + B - 1) / B;
@@ -523,6 +530,10 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
           uint32_t& s = (j & 1) ? seed1 : seed0;
           s = s * 1103515245u + 12345u;
           id = (int)(s % (uint32_t)np);
+        } else if (H > 1) {
+          const int h = pos / a.leaf_cap, s = pos - h * a.leaf_cap;
+          const int lf = h < H ? __ldg(a.hits + (size_t)q * H + h) : -1;
+          if (lf >= 0 && lf < a.n_leaves) id = __ldg(a.leaf_pids + (size_t)lf * a.leaf_cap + s);
         } else if (pos < n_first) {
           id = __ldg(lp + pos);
         } else if (hit2 >= 0 && pos < n_first + n_second) {

@@ -10,6 +10,7 @@ enum : int { kPrecF32 = 0, kPrecBF16 = 1, kPrecFP8 = 2 };
 // filter, 2*max(batch, beam) compaction slots, and a slot for the query's
 // BF16 row (tensor-core distances, up to 128 dims).
 constexpr int kQuerySlotWords = 64;
+constexpr int kMaxHits = 8;  // leaves per query for kd-tree entries
 
 struct SearchArgs {
   const float* base;        // lane-interleaved FP32 rows, stride 32*C floats
@@ -29,6 +30,7 @@ struct SearchArgs {
   int np, d, qstride, nq, R, W, k, max_iter, bloom_words, bloom_hashes, leaf_cap, entry_mode;
   int rerank;
   int n_leaves;             // hits outside [0, n_leaves) fall back to leaf 0
+  int max_hits;             // entry mode 1: hits holds [nq][max_hits] leaves (-1 padded)
   const int* nq_dev;        // if set, the query count is read here (graph replay)
 };
 

@@ -101,6 +101,7 @@ rte_status capture(rte_batcher* b) {
     a.entry_mode = b->prm.entry_mode;
     a.rerank = b->prm.rerank;
     a.n_leaves = x->has_kdtree ? (int)x->kd.n_leaves : 1;
+    a.max_hits = 1;
     e = launch_search(a, x->C, NL, NB, b->prm.precision, wpb, grid, smem, st);
   }
   cudaError_t e2 = cudaStreamEndCapture(st, &b->graph);
@@ -121,6 +122,7 @@ extern "C" rte_status rte_batcher_create(rte_index* x, int64_t max_nq,
   if (params->entry_mode == RTE_ENTRY_LEARNED)
     return fail(RTE_EINVAL, "the batcher serves random and kd-tree entries");
   if (params->rerank == 2) return fail(RTE_EINVAL, "the batcher does not rerank against the original rows");
+  if (params->max_hits > 1) return fail(RTE_EINVAL, "the batcher locates one leaf per query");
   DeviceGuard guard(x->device);
   auto* b = new rte_batcher();
   b->idx = x;

@@ -301,6 +301,31 @@ def test_truncated_pca_search_with_full_rerank(lib, orc, cuda, L):
         idx.search_projected(qp, beam=L, k=10, rerank=2)  # needs the original queries
 
 
+@pytest.mark.parametrize("H,L", [(2, 16), (4, 64), (3, 32)])
+def test_multi_leaf_entries_match_oracle(lib, orc, cuda, H, L):
+    """Kd-tree entries from the first H containing leaves (the reference's
+    disabled multi-hit entry): the leaves equal the oracle's H smallest
+    containing indices, and the search is bit-exact against the oracle."""
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(3000, 200, 128, True, seed=70 + H + L)
+    graph = ds.knn_graph(base, 64)
+    idx = _index(base, graph, 32, 0.2)
+    _, boxes, pids = idx.kdtree()
+    hm = idx.locate(q, max_hits=H)
+    assert np.array_equal(hm, orc.locate_multi(boxes, q[:, :3], H))
+    assert np.array_equal(hm[:, 0], idx.locate(q))
+    ids, dd = idx.search_projected(q, beam=L, k=L, max_hits=H)
+    oids, od = orc.search_multi(base, q, graph, L=L, k=L, hits_multi=hm, leaf_pids=pids)
+    assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
+    assert np.array_equal(dd, od)
+    # caller-given leaves, host and device, give the same result
+    ids2, _ = idx.search_projected(q, hits=hm, beam=L, k=L, max_hits=H)
+    assert np.array_equal(ids2, ids)
+    with pytest.raises(r.RteError):
+        idx.search_projected(q, beam=L, k=L, max_hits=H, entry_mode=r.ENTRY_RANDOM)
+
+
 def test_parameter_errors(lib, cuda):
     import rt_entry_gb300 as r
     from rt_entry_gb300 import datasets as ds
