@@ -125,8 +125,11 @@ __host__ __device__ constexpr int pool_regs(int NL) { return NL == 0 ? 1 : NL; }
 // 16 for the one-register beam-16 pool.  With DESC_FINAL the pair (a, a+sub)
 // is descending when a's 2*step block index is even, so the result is
 // descending, as the reference sorts its batch; otherwise the directions are
-// mirrored and the result is ascending.
-template <int NB, bool DESC_FINAL = true, int N = 32 * NB>
+// mirrored and the result is ascending.  Registers below KEEP_FROM are not
+// read after the sort (the merge reads only the last ones): the final step's
+// in-register stages skip them, which leaves every register that is read
+// unchanged.
+template <int NB, bool DESC_FINAL = true, int N = 32 * NB, int KEEP_FROM = 0>
 __device__ __forceinline__ void sort_batch_desc(float (&d)[NB], int (&id)[NB], int lane) {
   constexpr int B = N;
 #pragma unroll
@@ -144,6 +147,7 @@ __device__ __forceinline__ void sort_batch_desc(float (&d)[NB], int (&id)[NB], i
       } else {
 #pragma unroll
         for (int j = 0; j < NB; ++j) {
+          if (step == B / 2 && j < KEEP_FROM) continue;  // dead after the sort
           const bool desc = ((((j << 5) + lane) & (2 * step)) == 0) == DESC_FINAL;
           cx_lanes(d[j], id[j], sub, desc, lane);
         }
@@ -467,6 +471,8 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
                              float* s_dist, uint32_t* q_slot) {
   constexpr int L = pool_slots(NL);
   constexpr int PR = pool_regs(NL);  // pool registers
+  // the merge reads batch registers NB - min(PR, NB) .. NB-1 only
+  constexpr int kMergeFrom = NB - (PR < NB ? PR : NB);
   constexpr int B = 32 * NB;
   const int np = a.np;
   const int R = a.R;
@@ -545,7 +551,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     }
     __syncwarp();
     c_entries += batch_distances<C, NB, PREC>(a, qv, qx, bd, bi, s_ids, s_dist, lane);
-    sort_batch_desc<NB>(bd, bi, lane);
+    sort_batch_desc<NB, true, 32 * NB, kMergeFrom>(bd, bi, lane);
     merge_pool<NL, NB>(pd, pi, bd, bi, false, lane);
   }
 
@@ -639,7 +645,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     }
 
     c_dists += batch_distances<C, NB, PREC>(a, qv, qx, bd, bi, s_ids, s_dist, lane);
-    sort_batch_desc<NB>(bd, bi, lane);
+    sort_batch_desc<NB, true, 32 * NB, kMergeFrom>(bd, bi, lane);
     merge_pool<NL, NB>(pd, pi, bd, bi, true, lane);
 
     bool any = false;
