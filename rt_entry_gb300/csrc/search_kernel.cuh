@@ -59,15 +59,21 @@ struct Bloom {
   int lw;               // log2(words)
   int nh;
   // set_bit / test_bit: word x % SIZE, bit x / SIZE (graph_search.cuh:7-28).
+  // The loops are unrolled to the largest hash count (10), so each hash's
+  // multipliers are constant-bank operands.
   __device__ __forceinline__ void add(uint32_t x) const {
-    for (int h = 0; h < nh; ++h) {
+#pragma unroll
+    for (int h = 0; h < 10; ++h) {
+      if (h >= nh) break;
       uint32_t b = bloom_hash(h, x, bits_mask);
       atomicOr(&w[b & words_mask], 1u << (b >> lw));
     }
   }
   __device__ __forceinline__ bool test(uint32_t x) const {
     bool ok = true;
-    for (int h = 0; h < nh; ++h) {
+#pragma unroll
+    for (int h = 0; h < 10; ++h) {
+      if (h >= nh) break;
       uint32_t b = bloom_hash(h, x, bits_mask);
       ok &= ((w[b & words_mask] >> (b >> lw)) & 1u) != 0;
     }
@@ -477,6 +483,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
   const int np = a.np;
   const int R = a.R;
   const int NR = R >> 5;  // batch registers per expanded node
+  const int nr_shift = __ffs(NR) - 1;  // R is a power of two >= 32: j / NR == j >> nr_shift
   int c_entries = 0, c_expanded = 0, c_dists = 0;  // per query: far below 2^31
 
   float qv[C];
@@ -611,7 +618,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     // expands nothing (the reference would read past the graph)
 #pragma unroll
     for (int j = 0; j < NB; ++j) {
-      const int s = j / NR;
+      const int s = j >> nr_shift;
       int id = np;
       if (s < nsel) {
         const int node = pick<NB>(nodes, s);
@@ -629,12 +636,12 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
 #pragma unroll
       for (int j = 0; j < NB; ++j) {
         pass[j] = false;
-        if (j / NR == s) pass[j] = bi[j] != np && !bloom.test((uint32_t)bi[j]);
+        if ((j >> nr_shift) == s) pass[j] = bi[j] != np && !bloom.test((uint32_t)bi[j]);
       }
       __syncwarp();
 #pragma unroll
       for (int j = 0; j < NB; ++j) {
-        if (j / NR == s) {
+        if ((j >> nr_shift) == s) {
           if (pass[j])
             bloom.add((uint32_t)bi[j]);
           else
