@@ -47,7 +47,8 @@ bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 rte_status learned_leaves(const rte_index* x, const float* d_proj, int64_t nq, int32_t* d_leaf,
-                          cudaStream_t st, const uint16_t* xb_in = nullptr);
+                          cudaStream_t st, const uint16_t* xb_in = nullptr,
+                          unsigned long long* zkeys = nullptr, int* zerr = nullptr);
 }  // namespace rte
 
 namespace {
@@ -251,27 +252,54 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   if (full_rerank && already_projected)
     return fail(RTE_EINVAL, "rerank 2 needs the original queries: use rte_search");
   const float* qp = d_queries;
-  AsyncBuf proj, hitsb, work, xb;
+  AsyncBuf proj, hitsb, work, xb, zs;
   // learned entries without caller hits: the projection also writes the
   // model's BF16 input rows
   const bool head_input = prm->entry_mode == RTE_ENTRY_LEARNED && !d_hits_in && x->mlp.trained &&
                           x->mlp.d_in == x->search_dim;
-  if (!already_projected && x->has_pca) {
+  const bool projecting = !already_projected && x->has_pca;
+  // Scratch the projection zeroes on its way: the argmax keys (learned head),
+  // the head's error flag and the search's work counter, in that order.
+  const int64_t n_keys = projecting && head_input ? nq : 0;
+  unsigned long long* zkeys = nullptr;
+  int* zerr = nullptr;
+  unsigned int* zwork = nullptr;
+  if (projecting) {
+    RTE_CUDA(zs.alloc((size_t)n_keys * 8 + 8, st));
+    zkeys = n_keys ? zs.as<unsigned long long>() : nullptr;
+    zerr = reinterpret_cast<int*>(zs.as<char>() + n_keys * 8);
+    zwork = reinterpret_cast<unsigned int*>(zs.as<char>() + n_keys * 8 + 4);
+  }
+  const int32_t* hits2 = nullptr;
+  AsyncBuf hits2b;
+  SideStream* sd = nullptr;
+  // Any return after a fork waits for the side stream first, so that the
+  // buffers it writes are not freed (in stream order on st) under it.  The
+  // guard is declared after those buffers and so runs before their frees.
+  struct JoinGuard {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    ~JoinGuard() {
+      if (ev) cudaStreamWaitEvent(st, ev, 0);
+    }
+  } join_guard;
+  join_guard.st = st;
+  if (projecting) {
     RTE_CUDA(proj.alloc((size_t)nq * x->search_dim * 4, st));
+    const int64_t zwords = n_keys * 2 + 2;
     if (head_input) {
       RTE_CUDA(xb.alloc((size_t)nq * x->mlp.dp * 2, st));
       RTE_CUDA(launch_project_bf16(d_queries, nq, x->dim, x->dim, x->d_mean.p, x->d_rot.p,
                                    x->search_dim, x->search_dim, proj.as<float>(), x->search_dim,
-                                   xb.p, x->mlp.in_scale, x->mlp.dp, st));
+                                   xb.p, x->mlp.in_scale, x->mlp.dp, st, zs.as<uint32_t>(), zwords));
     } else {
       RTE_CUDA(launch_project(d_queries, nq, x->dim, x->dim, x->d_mean.p, x->d_rot.p,
-                              x->search_dim, x->search_dim, proj.as<float>(), x->search_dim, st));
+                              x->search_dim, x->search_dim, proj.as<float>(), x->search_dim, st,
+                              zs.as<uint32_t>(), zwords));
     }
     qp = proj.as<float>();
   }
   const int32_t* hits = d_hits_in;
-  const int32_t* hits2 = nullptr;
-  AsyncBuf hits2b;
   if (prm->entry_mode == RTE_ENTRY_KDTREE && !hits) {
     RTE_CUDA(hitsb.alloc((size_t)nq * prm->max_hits * 4, st));
     if (prm->max_hits > 1)
@@ -283,30 +311,40 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   }
   if (prm->entry_mode == RTE_ENTRY_LEARNED) {
     // proposed leaf (MLP) first, kd-tree leaf second; when the model runs
-    // here, the kd-tree location runs beside it on this thread's side stream
+    // here, the kd-tree location runs beside it on this thread's side
+    // stream, without shared memory so that its blocks fit beside the GEMMs
     RTE_CUDA(hits2b.alloc((size_t)nq * 4, st));
     hits2 = hits2b.as<int32_t>();
-    SideStream* sd = nullptr;
     const bool fork = !hits && side_stream(x->device, &sd) == cudaSuccess;
     if (fork) {
       RTE_CUDA(cudaEventRecord(sd->fork, st));
       RTE_CUDA(cudaStreamWaitEvent(sd->s, sd->fork, 0));
     }
-    RTE_CUDA(launch_locate(x->d_wide.p, (int)x->d_wide.n, qp, nq, x->search_dim,
-                           hits2b.as<int32_t>(), fork ? sd->s : st));
-    if (fork) RTE_CUDA(cudaEventRecord(sd->join, sd->s));
+    const cudaError_t le = launch_locate(x->d_wide.p, (int)x->d_wide.n, qp, nq, x->search_dim,
+                                         hits2b.as<int32_t>(), fork ? sd->s : st, /*top_cache=*/!fork);
+    if (fork) {
+      RTE_CUDA(cudaEventRecord(sd->join, sd->s));
+      join_guard.ev = sd->join;
+    }
+    RTE_CUDA(le);
     rte_status ls = RTE_OK;
     if (!hits) {
       RTE_CUDA(hitsb.alloc((size_t)nq * 4, st));
-      ls = learned_leaves(x, qp, nq, hitsb.as<int32_t>(), st, xb.p ? xb.as<uint16_t>() : nullptr);
+      ls = learned_leaves(x, qp, nq, hitsb.as<int32_t>(), st, xb.p ? xb.as<uint16_t>() : nullptr,
+                          zkeys, zkeys ? zerr : nullptr);
       hits = hitsb.as<int32_t>();
     }
     // join before anything returns: the buffers are freed in stream order on st
-    if (fork) RTE_CUDA(cudaStreamWaitEvent(st, sd->join, 0));
+    if (fork) {
+      join_guard.ev = nullptr;
+      RTE_CUDA(cudaStreamWaitEvent(st, sd->join, 0));
+    }
     if (ls != RTE_OK) return ls;
   }
-  RTE_CUDA(work.alloc(4, st));
-  RTE_CUDA(cudaMemsetAsync(work.p, 0, 4, st));
+  if (!zwork) {
+    RTE_CUDA(work.alloc(4, st));
+    RTE_CUDA(cudaMemsetAsync(work.p, 0, 4, st));
+  }
   AsyncBuf poolb;
   if (full_rerank) RTE_CUDA(poolb.alloc((size_t)nq * pl.L * 4, st));
   SearchArgs a{};
@@ -323,7 +361,7 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   a.out_ids = full_rerank ? poolb.as<int32_t>() : d_ids;
   a.out_dists = full_rerank ? nullptr : d_dists;
   a.counters = d_counters;
-  a.work = work.as<unsigned int>();
+  a.work = zwork ? zwork : work.as<unsigned int>();
   a.np = (int)x->np;
   a.d = x->search_dim;
   a.qstride = x->search_dim;

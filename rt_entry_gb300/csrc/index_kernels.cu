@@ -107,38 +107,52 @@ __global__ void cov_finish(const double* __restrict__ partial, int nchunks, int 
 
 // ---------------------------------------------------------- projection ----
 // out[r][j] = sum_c (x[r][c] - mean[c]) * V[c][j], one fmaf per c in
-// ascending order.  A block computes a 32 x 128 tile; each thread an 8 x 4
-// register tile, so every shared-memory read feeds 4 (x) or 8 (V) FMAs.  The
-// 32-wide slices of c are double-buffered: the next slice's global loads are
-// in flight while the current one is multiplied.  With kOut16 the block also
-// writes the learned head's BF16 input row: bf16(out * s16), zero-padded to
-// ld16 columns.
+// ascending order.  A block of 256 threads computes a 32 x 128 tile; warp w
+// owns rows 4w .. 4w+3 and lane l columns 4l .. 4l+3.  Shared memory keeps
+// each warp's four rows interleaved (sx[w][c][0..3]), so one broadcast
+// 16-byte load gives a thread its four x values and one 16-byte load its
+// four V values: two loads (five shared-memory wavefronts) per 16 FMAs.
+// The 64-wide slices of c are double-buffered in dynamic shared memory: the
+// next slice's global loads are in flight while the current one is
+// multiplied.  With kOut16 the block also writes the learned head's BF16
+// input row: bf16(out * s16), zero-padded to ld16 columns.
 constexpr int kPrRows = 32;
 constexpr int kPrCols = 128;
-constexpr int kPrK = 32;
+constexpr int kPrK = 64;
+constexpr int kPrThreads = 256;
+constexpr int kPrXFloats = kPrRows * kPrK;   // one buffer of sx
+constexpr int kPrVFloats = kPrK * kPrCols;   // one buffer of sv
+constexpr size_t kPrSmem = 2 * (size_t)(kPrXFloats + kPrVFloats) * 4;
 
 template <bool kOut16>
-__global__ void __launch_bounds__(128) project_rows(const float* __restrict__ x, int64_t n, int d,
-                                                    int xstride, const float* __restrict__ mean,
-                                                    const float* __restrict__ V, int vstride, int k,
-                                                    float* __restrict__ out, int ostride,
-                                                    const int* __restrict__ n_dev,
-                                                    __nv_bfloat16* __restrict__ out16, float s16,
-                                                    int ld16) {
+__global__ void __launch_bounds__(kPrThreads) project_rows(const float* __restrict__ x, int64_t n, int d,
+                                                           int xstride, const float* __restrict__ mean,
+                                                           const float* __restrict__ V, int vstride, int k,
+                                                           float* __restrict__ out, int ostride,
+                                                           const int* __restrict__ n_dev,
+                                                           __nv_bfloat16* __restrict__ out16, float s16,
+                                                           int ld16, uint32_t* __restrict__ zero,
+                                                           int64_t zero_words) {
+  if (zero) {  // the query call's counters and argmax keys, zeroed on the way
+    const int64_t nt = (int64_t)gridDim.x * gridDim.y * blockDim.x;
+    for (int64_t w = ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x; w < zero_words; w += nt)
+      zero[w] = 0u;
+  }
   if (n_dev) n = min(n, (int64_t)*n_dev);  // graph replay: rows beyond the batch are idle
   if ((int64_t)blockIdx.x * kPrRows >= n) return;
-  __shared__ float sx[2][kPrRows][kPrK + 1];
-  __shared__ __align__(16) float sv[2][kPrK][kPrCols];
+  extern __shared__ __align__(16) float pr_smem[];
+  float* sx = pr_smem;                    // [2][kPrRows/4][kPrK][4]
+  float* sv = pr_smem + 2 * kPrXFloats;   // [2][kPrK][kPrCols]
   const int64_t row0 = (int64_t)blockIdx.x * kPrRows;
   const int col0 = blockIdx.y * kPrCols;
   const int tx = threadIdx.x & 31;  // columns 4tx .. 4tx+3
-  const int ty = threadIdx.x >> 5;  // rows 8ty .. 8ty+7
-  constexpr int kXPer = kPrRows * kPrK / 128, kVPer = kPrK * kPrCols / 128;
+  const int ty = threadIdx.x >> 5;  // rows 4ty .. 4ty+3
+  constexpr int kXPer = kPrXFloats / kPrThreads, kVPer = kPrVFloats / kPrThreads;
   float rx[kXPer], rv[kVPer];
   auto gload = [&](int c0) {
 #pragma unroll
     for (int u = 0; u < kXPer; ++u) {
-      const int t = threadIdx.x + 128 * u;
+      const int t = threadIdx.x + kPrThreads * u;
       const int rr = t / kPrK, cc = t % kPrK;
       const int64_t r = row0 + rr;
       float v = 0.0f;
@@ -147,7 +161,8 @@ __global__ void __launch_bounds__(128) project_rows(const float* __restrict__ x,
     }
 #pragma unroll
     for (int u = 0; u < kVPer; ++u) {
-      const int cc = u, jj = threadIdx.x;  // t = threadIdx.x + 128u over a 32 x 128 slice
+      const int t = threadIdx.x + kPrThreads * u;
+      const int cc = t / kPrCols, jj = t % kPrCols;
       float v = 0.0f;
       if (c0 + cc < d && col0 + jj < k) v = V[(int64_t)(c0 + cc) * vstride + col0 + jj];
       rv[u] = v;
@@ -156,15 +171,16 @@ __global__ void __launch_bounds__(128) project_rows(const float* __restrict__ x,
   auto sstore = [&](int b) {
 #pragma unroll
     for (int u = 0; u < kXPer; ++u) {
-      const int t = threadIdx.x + 128 * u;
-      sx[b][t / kPrK][t % kPrK] = rx[u];
+      const int t = threadIdx.x + kPrThreads * u;
+      const int rr = t / kPrK, cc = t % kPrK;
+      sx[b * kPrXFloats + ((rr >> 2) * kPrK + cc) * 4 + (rr & 3)] = rx[u];
     }
 #pragma unroll
-    for (int u = 0; u < kVPer; ++u) sv[b][u][threadIdx.x] = rv[u];
+    for (int u = 0; u < kVPer; ++u) sv[b * kPrVFloats + threadIdx.x + kPrThreads * u] = rv[u];
   };
-  float acc[8][4];
+  float acc[4][4];
 #pragma unroll
-  for (int i = 0; i < 8; ++i)
+  for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
   gload(0);
@@ -174,34 +190,63 @@ __global__ void __launch_bounds__(128) project_rows(const float* __restrict__ x,
   for (int c0 = 0; c0 < d; c0 += kPrK) {
     const bool more = c0 + kPrK < d;
     if (more) gload(c0 + kPrK);
+    const float4* xs = reinterpret_cast<const float4*>(sx + b * kPrXFloats) + ty * kPrK;
+    const float4* vs = reinterpret_cast<const float4*>(sv + b * kPrVFloats) + tx;
 #pragma unroll 8
     for (int cc = 0; cc < kPrK; ++cc) {
-      const float4 v = *reinterpret_cast<const float4*>(&sv[b][cc][4 * tx]);
+      const float4 xv = xs[cc];
+      const float4 v = vs[cc * (kPrCols / 4)];
+      const float xr[4] = {xv.x, xv.y, xv.z, xv.w};
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const float xv = sx[b][8 * ty + i][cc];
-        acc[i][0] = __fmaf_rn(xv, v.x, acc[i][0]);
-        acc[i][1] = __fmaf_rn(xv, v.y, acc[i][1]);
-        acc[i][2] = __fmaf_rn(xv, v.z, acc[i][2]);
-        acc[i][3] = __fmaf_rn(xv, v.w, acc[i][3]);
+      for (int i = 0; i < 4; ++i) {
+        acc[i][0] = __fmaf_rn(xr[i], v.x, acc[i][0]);
+        acc[i][1] = __fmaf_rn(xr[i], v.y, acc[i][1]);
+        acc[i][2] = __fmaf_rn(xr[i], v.z, acc[i][2]);
+        acc[i][3] = __fmaf_rn(xr[i], v.w, acc[i][3]);
       }
     }
     if (more) sstore(b ^ 1);
     __syncthreads();
     b ^= 1;
   }
+  const int c4 = col0 + 4 * tx;
+  const bool vec32 = (ostride & 3) == 0 && ((uintptr_t)out & 15) == 0 && c4 + 3 < k;
+  const bool vec16 = kOut16 && (ld16 & 3) == 0 && ((uintptr_t)out16 & 7) == 0 && c4 + 3 < ld16;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int64_t r = row0 + 8 * ty + i;
+  for (int i = 0; i < 4; ++i) {
+    const int64_t r = row0 + 4 * ty + i;
     if (r >= n) break;
+    if (vec32) {
+      *reinterpret_cast<float4*>(out + r * ostride + c4) = make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+    } else {
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int col = col0 + 4 * tx + j;
-      if (col < k) out[r * ostride + col] = acc[i][j];
+      for (int j = 0; j < 4; ++j)
+        if (c4 + j < k) out[r * ostride + c4 + j] = acc[i][j];
+    }
+    if (kOut16) {
       // acc is 0 in the padding columns k .. ld16-1
-      if (kOut16 && col < ld16) out16[r * ld16 + col] = __float2bfloat16_rn(__fmul_rn(acc[i][j], s16));
+      __nv_bfloat16 h[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) h[j] = __float2bfloat16_rn(__fmul_rn(acc[i][j], s16));
+      if (vec16) {
+        uint2 u;
+        u.x = (uint32_t)__bfloat16_as_ushort(h[0]) | ((uint32_t)__bfloat16_as_ushort(h[1]) << 16);
+        u.y = (uint32_t)__bfloat16_as_ushort(h[2]) | ((uint32_t)__bfloat16_as_ushort(h[3]) << 16);
+        *reinterpret_cast<uint2*>(out16 + r * ld16 + c4) = u;
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (c4 + j < ld16) out16[r * ld16 + c4 + j] = h[j];
+      }
     }
   }
+}
+
+// The projection's dynamic shared memory is above the 48 KB default.
+template <bool kOut16>
+cudaError_t project_smem_attr() {
+  return cudaFuncSetAttribute(project_rows<kOut16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kPrSmem);
 }
 
 // ---------------------------------------------------------- interleave ----
@@ -288,6 +333,7 @@ __global__ void dequant_rows(const void* __restrict__ il, const float* __restric
 // levels, nine binary levels) are copied into shared memory by every block.
 constexpr int kTopWide = 73;
 constexpr int kLocStack = 64;
+constexpr int64_t kTreePrefetchLines = (32ll << 20) / 128;  // at most the first 32 MB
 
 // One wide-tree step shared by the locate kernels: the containing children of
 // wide node w pushed last-first onto the stack.
@@ -318,14 +364,42 @@ __device__ __forceinline__ void push_containing(const WideNode* w, bool shared_c
 }
 
 
+// The first three coordinates of point i (rows of `stride` floats; a search
+// space of fewer than three dimensions has zeros beyond them, as the kd-tree
+// build pads them).
+__device__ __forceinline__ void load_xyz(const float* __restrict__ pts, int64_t i, int stride, float& x,
+                                         float& y, float& z) {
+  const float* p = pts + i * stride;
+  x = p[0];
+  y = stride > 1 ? p[1] : 0.0f;
+  z = stride > 2 ? p[2] : 0.0f;
+}
+
+// Requests the first `lines` 128-byte lines of the wide tree into L2, spread
+// over the grid's threads, so that the searches' deeper levels find their
+// nodes in L2 rather than in DRAM.
+__device__ __forceinline__ void prefetch_tree(const WideNode* wide, int n_wide) {
+  const int64_t lines = min((int64_t)n_wide * (int64_t)sizeof(WideNode) / 128, (int64_t)kTreePrefetchLines);
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nt = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t l = t; l < lines; l += nt)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char*>(wide) + l * 128));
+}
+
+// kTop: the first kTopWide nodes are copied into shared memory by every
+// block.  Without it the kernel uses no shared memory, so its blocks can sit
+// beside a kernel that takes most of an SM's shared memory (the learned
+// head's GEMMs, which it runs beside).
+template <bool kTop>
 __global__ void locate_points(const WideNode* __restrict__ wide, int n_wide,
                               const float* __restrict__ pts, int64_t n, int stride,
                               int32_t* __restrict__ out, const int* __restrict__ n_dev) {
-  __shared__ WideNode top[kTopWide];
+  __shared__ WideNode top[kTop ? kTopWide : 1];
   if (n_dev) n = min(n, (int64_t)*n_dev);
   if ((int64_t)blockIdx.x * blockDim.x >= n) return;
-  const int ntop = min(kTopWide, n_wide);
-  {
+  prefetch_tree(wide, n_wide);
+  const int ntop = kTop ? min(kTopWide, n_wide) : 0;
+  if (kTop) {
     const float4* src = reinterpret_cast<const float4*>(wide);
     float4* dst = reinterpret_cast<float4*>(top);
     for (int i = threadIdx.x; i < 16 * ntop; i += blockDim.x) dst[i] = __ldg(src + i);
@@ -333,7 +407,8 @@ __global__ void locate_points(const WideNode* __restrict__ wide, int n_wide,
   }
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float x = pts[i * stride + 0], y = pts[i * stride + 1], z = pts[i * stride + 2];
+  float x, y, z;
+  load_xyz(pts, i, stride, x, y, z);
   int stack[kLocStack];
   int sp = 0;
   stack[sp++] = 0;
@@ -349,8 +424,6 @@ __global__ void locate_points(const WideNode* __restrict__ wide, int n_wide,
   out[i] = hit;
 }
 
-// The first H containing leaves in pre-order (the H smallest indices), -1
-// padded; leaf 0 first when none contains the point.  The same search as
 // locate_points, continued past the first leaf.
 __global__ void locate_points_multi(const WideNode* __restrict__ wide, int n_wide,
                                     const float* __restrict__ pts, int64_t n, int stride, int H,
@@ -366,7 +439,8 @@ __global__ void locate_points_multi(const WideNode* __restrict__ wide, int n_wid
   }
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float x = pts[i * stride + 0], y = pts[i * stride + 1], z = pts[i * stride + 2];
+  float x, y, z;
+  load_xyz(pts, i, stride, x, y, z);
   int stack[kLocStack];
   int sp = 0;
   stack[sp++] = 0;
@@ -395,7 +469,8 @@ __global__ void locate_in_subtree_wide(const WideNode* __restrict__ wide,
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int c = 0x7fffffff - (int)(keys[i] & 0xffffffffu);
-  const float x = pts[i * stride + 0], y = pts[i * stride + 1], z = pts[i * stride + 2];
+  float x, y, z;
+  load_xyz(pts, i, stride, x, y, z);
   int stack[kLocStack];
   int sp = 0;
   stack[sp++] = start_ref[c];
@@ -425,7 +500,8 @@ __global__ void locate_in_subtree(const BvhNode* __restrict__ nodes, const float
   if (i >= n) return;
   // the class is given, or decoded from the packed argmax key (gemm_tc.h)
   const int c = keys ? 0x7fffffff - (int)(keys[i] & 0xffffffffu) : cls[i];
-  const float x = pts[i * stride + 0], y = pts[i * stride + 1], z = pts[i * stride + 2];
+  float x, y, z;
+  load_xyz(pts, i, stride, x, y, z);
   int stack[kBvhMaxDepth];
   int sp = 0;
   stack[sp++] = start_node[c];
@@ -497,22 +573,28 @@ cudaError_t launch_cov(const float* x, int64_t n, int d, const double* mean, dou
 
 cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const float* mean,
                            const float* V, int vstride, int k, float* out, int ostride,
-                           cudaStream_t st) {
+                           cudaStream_t st, uint32_t* zero, int64_t zero_words) {
   if (n == 0) return cudaSuccess;
   dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  project_rows<false><<<grid, 128, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride,
-                                            nullptr, nullptr, 0.0f, 0);
+  cudaError_t e = project_smem_attr<false>();
+  if (e != cudaSuccess) return e;
+  project_rows<false><<<grid, kPrThreads, kPrSmem, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride,
+                                            nullptr, nullptr, 0.0f, 0, zero, zero_words);
   return cudaGetLastError();
 }
 
 cudaError_t launch_project_bf16(const float* x, int64_t n, int d, int xstride, const float* mean,
                                 const float* V, int vstride, int k, float* out, int ostride,
-                                void* out16, float s16, int ld16, cudaStream_t st) {
+                                void* out16, float s16, int ld16, cudaStream_t st, uint32_t* zero,
+                                int64_t zero_words) {
   if (n == 0) return cudaSuccess;
   if (ld16 < k || ld16 > ((k + kPrCols - 1) / kPrCols) * kPrCols) return cudaErrorInvalidValue;
   dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  project_rows<true><<<grid, 128, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr,
-                                           reinterpret_cast<__nv_bfloat16*>(out16), s16, ld16);
+  cudaError_t e = project_smem_attr<true>();
+  if (e != cudaSuccess) return e;
+  project_rows<true><<<grid, kPrThreads, kPrSmem, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr,
+                                           reinterpret_cast<__nv_bfloat16*>(out16), s16, ld16, zero,
+                                           zero_words);
   return cudaGetLastError();
 }
 
@@ -520,8 +602,10 @@ cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, in
                                const float* mean, const float* V, int vstride, int k, float* out,
                                int ostride, cudaStream_t st) {
   dim3 grid((unsigned)((cap + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  project_rows<false><<<grid, 128, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride,
-                                            n_dev, nullptr, 0.0f, 0);
+  cudaError_t e = project_smem_attr<false>();
+  if (e != cudaSuccess) return e;
+  project_rows<false><<<grid, kPrThreads, kPrSmem, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride,
+                                            n_dev, nullptr, 0.0f, 0, nullptr, 0);
   return cudaGetLastError();
 }
 
@@ -576,15 +660,18 @@ cudaError_t launch_locate_multi(const WideNode* wide, int n_wide, const float* p
 }
 
 cudaError_t launch_locate(const WideNode* wide, int n_wide, const float* pts, int64_t n, int stride,
-                          int32_t* out, cudaStream_t st) {
+                          int32_t* out, cudaStream_t st, bool top_cache) {
   if (n == 0) return cudaSuccess;
-  locate_points<<<(unsigned)((n + 63) / 64), 64, 0, st>>>(wide, n_wide, pts, n, stride, out, nullptr);
+  if (top_cache)
+    locate_points<true><<<(unsigned)((n + 63) / 64), 64, 0, st>>>(wide, n_wide, pts, n, stride, out, nullptr);
+  else
+    locate_points<false><<<(unsigned)((n + 63) / 64), 64, 0, st>>>(wide, n_wide, pts, n, stride, out, nullptr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_locate_dyn(const WideNode* wide, int n_wide, const float* pts, int64_t cap,
                               const int* n_dev, int stride, int32_t* out, cudaStream_t st) {
-  locate_points<<<(unsigned)((cap + 63) / 64), 64, 0, st>>>(wide, n_wide, pts, cap, stride, out, n_dev);
+  locate_points<true><<<(unsigned)((cap + 63) / 64), 64, 0, st>>>(wide, n_wide, pts, cap, stride, out, n_dev);
   return cudaGetLastError();
 }
 

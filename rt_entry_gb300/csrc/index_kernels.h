@@ -38,15 +38,19 @@ cudaError_t launch_mean(const float* x, int64_t n, int d, double* partial, int n
                         double* mean, cudaStream_t st);
 cudaError_t launch_cov(const float* x, int64_t n, int d, const double* mean, double* partial,
                        int nchunks, double* cov, cudaStream_t st);
+// zero / zero_words: a word range the kernel also sets to 0 (a query call's
+// work counter, error flag and argmax keys), so that the call needs no
+// separate memsets.
 cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const float* mean,
                            const float* V, int vstride, int k, float* out, int ostride,
-                           cudaStream_t st);
+                           cudaStream_t st, uint32_t* zero = nullptr, int64_t zero_words = 0);
 // launch_project plus a BF16 copy of the output: out16[r][c] =
 // bf16(out[r][c] * s16) for c < k, 0 for k <= c < ld16 (the learned head's
 // input rows, ld16 >= k).
 cudaError_t launch_project_bf16(const float* x, int64_t n, int d, int xstride, const float* mean,
                                 const float* V, int vstride, int k, float* out, int ostride,
-                                void* out16, float s16, int ld16, cudaStream_t st);
+                                void* out16, float s16, int ld16, cudaStream_t st,
+                                uint32_t* zero = nullptr, int64_t zero_words = 0);
 // Variants for graph replay: grids sized for `cap` rows, the live row count
 // read from device memory at run time.
 cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, int d, int xstride,
@@ -79,7 +83,10 @@ cudaError_t launch_locate_in_subtree_wide(const WideNode* wide, const float* pts
 // a miss).
 cudaError_t launch_locate_multi(const WideNode* wide, int n_wide, const float* pts, int64_t n,
                                 int stride, int H, int32_t* out, cudaStream_t st);
+// top_cache: copy the top of the tree into each block's shared memory; off
+// when the launch runs beside a kernel that needs most of an SM's shared
+// memory.
 cudaError_t launch_locate(const WideNode* wide, int n_wide, const float* pts, int64_t n, int stride,
-                          int32_t* out, cudaStream_t st);
+                          int32_t* out, cudaStream_t st, bool top_cache = true);
 
 }  // namespace rte

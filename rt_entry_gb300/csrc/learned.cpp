@@ -154,14 +154,14 @@ cudaError_t gemm(const void* A, const void* B, int M, int N, int K, int epi, voi
 int round8(int v) { return (v + 7) & ~7; }
 
 // MLP forward for nq rows of X (BF16 [nq x dp]) -> packed argmax key per row
-// (keys [nq], zeroed here).
+// (keys [nq], zeroed here unless keys_zeroed).
 rte_status mlp_keys_bf16(const rte_index* x, const uint16_t* X, int64_t nq, unsigned long long* keys,
-                         int* d_err, cudaStream_t st) {
+                         int* d_err, cudaStream_t st, bool keys_zeroed) {
   const Mlp& m = x->mlp;
   AsyncBuf h1, h2;
   RTE_CUDA(h1.alloc((size_t)nq * m.hidden * 2, st));
   RTE_CUDA(h2.alloc((size_t)nq * m.hidden * 2, st));
-  RTE_CUDA(cudaMemsetAsync(keys, 0, (size_t)nq * 8, st));
+  if (!keys_zeroed) RTE_CUDA(cudaMemsetAsync(keys, 0, (size_t)nq * 8, st));
   RTE_CUDA(gemm(X, m.W16[0].p, (int)nq, m.hidden, m.dp, kEpiBiasReluBF16, h1.p, m.hidden, m.b[0].p,
                 nullptr, d_err, st));
   RTE_CUDA(gemm(h1.p, m.W16[1].p, (int)nq, m.hidden, m.hidden, kEpiBiasReluBF16, h2.p, m.hidden,
@@ -176,7 +176,7 @@ rte_status mlp_predict_bf16(const rte_index* x, const uint16_t* X, int64_t nq, i
                             int* d_err, cudaStream_t st) {
   AsyncBuf keys;
   RTE_CUDA(keys.alloc((size_t)nq * 8, st));
-  rte_status s = mlp_keys_bf16(x, X, nq, keys.as<unsigned long long>(), d_err, st);
+  rte_status s = mlp_keys_bf16(x, X, nq, keys.as<unsigned long long>(), d_err, st, false);
   if (s != RTE_OK) return s;
   RTE_CUDA(launch_argmax_to_leaf(keys.as<unsigned long long>(), (int)nq, nullptr, d_cls, st));
   return RTE_OK;
@@ -287,31 +287,39 @@ namespace rte {
 // xb: the head's BF16 input rows ([nq x dp], from launch_project_bf16), or
 // null to form them here from d_proj.
 rte_status learned_leaves(const rte_index* x, const float* d_proj, int64_t nq, int32_t* d_leaf,
-                          cudaStream_t st, const uint16_t* xb_in) {
+                          cudaStream_t st, const uint16_t* xb_in, unsigned long long* zkeys, int* zerr) {
   if (!x->mlp.trained) return fail(RTE_ESTATE, "learned entries requested before rte_learned_train");
   if (nq == 0) return RTE_OK;
   const Mlp& m = x->mlp;
-  AsyncBuf xb, err, keys;
-  RTE_CUDA(err.alloc(4, st));
-  RTE_CUDA(cudaMemsetAsync(err.p, 0, 4, st));
+  AsyncBuf xb, errb, keysb;
+  // zkeys / zerr: scratch the caller has already zeroed
+  const bool zeroed = zkeys && zerr;
+  int* err = zerr;
+  unsigned long long* keys = zkeys;
+  if (!zeroed) {
+    RTE_CUDA(errb.alloc(4, st));
+    RTE_CUDA(cudaMemsetAsync(errb.p, 0, 4, st));
+    RTE_CUDA(keysb.alloc((size_t)nq * 8, st));
+    err = errb.as<int>();
+    keys = keysb.as<unsigned long long>();
+  }
   const uint16_t* X = xb_in;
   if (!X) {
     RTE_CUDA(xb.alloc((size_t)nq * m.dp * 2, st));
     RTE_CUDA(launch_cast_rows_bf16(d_proj, nq, m.d_in, x->search_dim, m.in_scale, m.dp, xb.p, st));
     X = xb.as<uint16_t>();
   }
-  RTE_CUDA(keys.alloc((size_t)nq * 8, st));
-  rte_status s = mlp_keys_bf16(x, X, nq, keys.as<unsigned long long>(), err.as<int>(), st);
+  rte_status s = mlp_keys_bf16(x, X, nq, keys, err, st, zeroed);
   if (s != RTE_OK) return s;
   // the model picks the subtree (decoded from its argmax key), the kd-tree
   // picks the leaf inside it
   if (m.class_wide.p) {
     RTE_CUDA(launch_locate_in_subtree_wide(x->d_wide.p, d_proj, nq, x->search_dim,
-                                           keys.as<unsigned long long>(), m.class_wide.p,
+                                           keys, m.class_wide.p,
                                            m.class_leaf0.p, d_leaf, st));
   } else {
     RTE_CUDA(launch_locate_in_subtree(x->d_nodes.p, d_proj, nq, x->search_dim, nullptr,
-                                      keys.as<unsigned long long>(), m.class_node.p,
+                                      keys, m.class_node.p,
                                       m.class_leaf0.p, d_leaf, st));
   }
   return RTE_OK;
@@ -566,7 +574,7 @@ extern "C" rte_status rte_learned_predict(rte_index* x, const float* projected, 
     RTE_CUDA(ob.alloc((size_t)nq * 4, st));
     dout = ob.as<int32_t>();
   }
-  rte_status s = learned_leaves(x, dp, nq, dout, st, nullptr);
+  rte_status s = learned_leaves(x, dp, nq, dout, st, nullptr, nullptr, nullptr);
   if (s != RTE_OK) return s;
   if (host_out) {
     RTE_CUDA(cudaMemcpyAsync(out_leaf, dout, (size_t)nq * 4, cudaMemcpyDeviceToHost, st));

@@ -1,7 +1,7 @@
 """Profiling driver: the search kernel on the benchmark's index, few launches.
 
     python -m rt_entry_gb300.profile_search [--nq 2000] [--precision 0|1|2] [--beam 64]
-                                            [--entry 1|2] [--rerank 0|1]
+                                            [--entry 1|2] [--rerank 0|1] [--raw]
 
 Builds the 1M x 128 benchmark index (same generator, seeds and graph as
 bench.py), then launches the search kernel exactly twice on `nq` queries:
@@ -11,7 +11,10 @@ one warm-up launch and one launch to capture, e.g.
         -o prof python -m rt_entry_gb300.profile_search --nq 2000
 
 Prints the event-timed duration and the algorithmic bytes of the second
-launch so that ncu's DRAM bytes can be set against them.
+launch so that ncu's DRAM bytes can be set against them.  With --raw both
+calls go through the public path from raw queries (projection, entry
+location, learned head, search), so every kernel of a query call can be
+captured.
 """
 from __future__ import annotations
 
@@ -43,6 +46,7 @@ def main():
     ap.add_argument("--width", type=int, default=1)
     ap.add_argument("--entry", type=int, default=1)
     ap.add_argument("--rerank", type=int, default=0)
+    ap.add_argument("--raw", action="store_true", help="the whole query call from raw queries")
     a = ap.parse_args()
     rbuild.build()
     w = ds.make_config(2, nq=a.nq, with_gt=False, device="cuda")
@@ -54,12 +58,20 @@ def main():
     hits = idx.locate(qp)
     p = r.default_params(beam=a.beam, k=10, search_width=a.width, precision=a.precision,
                          rerank=a.rerank, entry_mode=a.entry)
-    idx.search_projected(qp, hits=hits if a.entry == 1 else None, params=p)  # warm-up launch
+    qd = torch.from_numpy(w.queries).cuda()
+
+    def call():
+        if a.raw:
+            idx.search(qd, params=p)
+        else:
+            idx.search_projected(qp, hits=hits if a.entry == 1 else None, params=p)
+
+    call()  # warm-up launch
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.nvtx.range_push("rte_profiled")  # lets a profiler select this launch
     e0.record()
-    idx.search_projected(qp, hits=hits if a.entry == 1 else None, params=p)  # profiled launch
+    call()  # profiled launch
     e1.record()
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
