@@ -112,20 +112,21 @@ __global__ void cov_finish(const double* __restrict__ partial, int nchunks, int 
 // each warp's four rows interleaved (sx[w][c][0..3]), so one broadcast
 // 16-byte load gives a thread its four x values and one 16-byte load its
 // four V values: two loads (five shared-memory wavefronts) per 16 FMAs.
-// The 64-wide slices of c are double-buffered in dynamic shared memory: the
+// The 32-wide slices of c are double-buffered in shared memory (40 KB): the
 // next slice's global loads are in flight while the current one is
-// multiplied.  With kOut16 the block also writes the learned head's BF16
-// input row: bf16(out * s16), zero-padded to ld16 columns.
+// multiplied.  At most 85 registers a thread keep three blocks on an SM, so
+// a batch of up to 152 x 3 x 32 rows runs in a single wave.  With kOut16 the
+// block also writes the learned head's BF16 input row: bf16(out * s16),
+// zero-padded to ld16 columns.
 constexpr int kPrRows = 32;
 constexpr int kPrCols = 128;
-constexpr int kPrK = 64;
+constexpr int kPrK = 32;
 constexpr int kPrThreads = 256;
 constexpr int kPrXFloats = kPrRows * kPrK;   // one buffer of sx
 constexpr int kPrVFloats = kPrK * kPrCols;   // one buffer of sv
-constexpr size_t kPrSmem = 2 * (size_t)(kPrXFloats + kPrVFloats) * 4;
 
 template <bool kOut16>
-__global__ void __launch_bounds__(kPrThreads) project_rows(const float* __restrict__ x, int64_t n, int d,
+__global__ void __launch_bounds__(kPrThreads, 3) project_rows(const float* __restrict__ x, int64_t n, int d,
                                                            int xstride, const float* __restrict__ mean,
                                                            const float* __restrict__ V, int vstride, int k,
                                                            float* __restrict__ out, int ostride,
@@ -140,7 +141,7 @@ __global__ void __launch_bounds__(kPrThreads) project_rows(const float* __restri
   }
   if (n_dev) n = min(n, (int64_t)*n_dev);  // graph replay: rows beyond the batch are idle
   if ((int64_t)blockIdx.x * kPrRows >= n) return;
-  extern __shared__ __align__(16) float pr_smem[];
+  __shared__ __align__(16) float pr_smem[2 * (kPrXFloats + kPrVFloats)];
   float* sx = pr_smem;                    // [2][kPrRows/4][kPrK][4]
   float* sv = pr_smem + 2 * kPrXFloats;   // [2][kPrK][kPrCols]
   const int64_t row0 = (int64_t)blockIdx.x * kPrRows;
@@ -240,13 +241,6 @@ __global__ void __launch_bounds__(kPrThreads) project_rows(const float* __restri
       }
     }
   }
-}
-
-// The projection's dynamic shared memory is above the 48 KB default.
-template <bool kOut16>
-cudaError_t project_smem_attr() {
-  return cudaFuncSetAttribute(project_rows<kOut16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)kPrSmem);
 }
 
 // ---------------------------------------------------------- interleave ----
@@ -576,9 +570,7 @@ cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const 
                            cudaStream_t st, uint32_t* zero, int64_t zero_words) {
   if (n == 0) return cudaSuccess;
   dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  cudaError_t e = project_smem_attr<false>();
-  if (e != cudaSuccess) return e;
-  project_rows<false><<<grid, kPrThreads, kPrSmem, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride,
+  project_rows<false><<<grid, kPrThreads, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride,
                                             nullptr, nullptr, 0.0f, 0, zero, zero_words);
   return cudaGetLastError();
 }
@@ -590,9 +582,7 @@ cudaError_t launch_project_bf16(const float* x, int64_t n, int d, int xstride, c
   if (n == 0) return cudaSuccess;
   if (ld16 < k || ld16 > ((k + kPrCols - 1) / kPrCols) * kPrCols) return cudaErrorInvalidValue;
   dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  cudaError_t e = project_smem_attr<true>();
-  if (e != cudaSuccess) return e;
-  project_rows<true><<<grid, kPrThreads, kPrSmem, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr,
+  project_rows<true><<<grid, kPrThreads, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr,
                                            reinterpret_cast<__nv_bfloat16*>(out16), s16, ld16, zero,
                                            zero_words);
   return cudaGetLastError();
@@ -602,9 +592,7 @@ cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, in
                                const float* mean, const float* V, int vstride, int k, float* out,
                                int ostride, cudaStream_t st) {
   dim3 grid((unsigned)((cap + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
-  cudaError_t e = project_smem_attr<false>();
-  if (e != cudaSuccess) return e;
-  project_rows<false><<<grid, kPrThreads, kPrSmem, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride,
+  project_rows<false><<<grid, kPrThreads, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride,
                                             n_dev, nullptr, 0.0f, 0, nullptr, 0);
   return cudaGetLastError();
 }
