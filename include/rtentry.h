@@ -309,6 +309,19 @@ rte_status rte_gemm_bf16(const uint16_t* A, const uint16_t* B, int M, int N, int
 rte_status rte_gemm_bf16_bias_argmax(const uint16_t* A, const uint16_t* B, const float* bias, int M,
                                      int N, int K, int32_t* cols, void* stream);
 
+/* The learned head's whole forward pass: for each row m of X [M x dp], the
+ * column n of the largest (relu(relu(X W1^T + b1) W2^T + b2) W3^T + b3)[m][n]
+ * (the first on ties), the hidden activations rounded to BF16.  W1 [H x dp],
+ * W2 [H x H], W3 [N x H], X: BF16 bit patterns, row-major; biases FP32.
+ * path 0: the fused single-kernel form rte_search uses (H a multiple of 64
+ * up to 256, dp up to 256; RTE_EINVAL otherwise); path 1: the three
+ * layer-by-layer GEMMs.  Both give the same columns.  Device pointers;
+ * cols [M] int32.  RTE_ETIMEOUT if a bounded pipeline wait ran out.  (No
+ * reference counterpart.) */
+rte_status rte_mlp_head_argmax(const uint16_t* X, int M, int dp, const uint16_t* W1, const float* b1,
+                               const uint16_t* W2, const float* b2, const uint16_t* W3, const float* b3,
+                               int H, int N, int path, int32_t* cols, void* stream);
+
 /* The first max_hits (1..8) leaves whose expanded boxes contain each
  * projected query, smallest index first, -1 padded; a query in no box gets
  * leaf 0 first.  out [nq x max_hits].  Host or device pointers.  The entry

@@ -31,7 +31,7 @@ EXPORTS = (
     "rte_get_kdtree", "rte_index_save", "rte_index_load_dir", "rte_index_free", "rte_last_error",
     "rte_kdtree_build_host", "rte_sym_eig_host", "rte_get_search_base_lowp", "rte_gemm_bf16",
     "rte_default_train_params", "rte_learned_train", "rte_learned_predict", "rte_mlp_grad_check",
-    "rte_search_projected_noalloc", "rte_gemm_bf16_bias_argmax", "rte_knn_graph", "rte_locate_multi", "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
+    "rte_search_projected_noalloc", "rte_gemm_bf16_bias_argmax", "rte_mlp_head_argmax", "rte_knn_graph", "rte_locate_multi", "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
     "rte_batcher_free", "rte_autotune",
 )
 
@@ -123,6 +123,7 @@ def load_library(path: str = LIB_PATH):
         "rte_get_search_base_lowp": ([P, i32, P], i32),
         "rte_gemm_bf16": ([P, P, i32, i32, i32, P, P], i32),
         "rte_gemm_bf16_bias_argmax": ([P, P, P, i32, i32, i32, P, P], i32),
+        "rte_mlp_head_argmax": ([P, i32, i32, P, P, P, P, P, P, i32, i32, i32, P, P], i32),
         "rte_knn_graph": ([P, i64, i32, i32, i32, P, P], i32),
         "rte_locate_multi": ([P, P, i64, i32, P, P], i32),
         "rte_default_train_params": ([ctypes.POINTER(TrainParams)], None),
@@ -259,6 +260,26 @@ def gemm_bf16_bias_argmax(a_bits, b_bits, bias):
         a.ctypes.data_as(ctypes.c_void_p), b.ctypes.data_as(ctypes.c_void_p),
         bias.ctypes.data_as(ctypes.c_void_p), M, N, K, out.ctypes.data_as(ctypes.c_void_p), None))
     return out
+
+
+def mlp_head_argmax(x, w1, b1, w2, b2, w3, b3, path: int = 0, stream=None):
+    """Row argmax of the learned head's forward pass on device tensors:
+    x [M, dp], w1 [H, dp], w2 [H, H], w3 [N, H] BF16 (torch.bfloat16 or
+    int16/uint16 bit patterns), biases FP32.  path 0 is the fused kernel,
+    path 1 the three layer-by-layer GEMMs.  Returns cols [M] int32 on the
+    device."""
+    import torch
+    ts = [x, w1, b1, w2, b2, w3, b3]
+    for t in ts:
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.is_contiguous()):
+            raise ValueError("mlp_head_argmax takes contiguous CUDA tensors")
+    M, dp = x.shape
+    H, N = w1.shape[0], w3.shape[0]
+    cols = torch.empty(M, dtype=torch.int32, device=x.device)
+    _check(load_library().rte_mlp_head_argmax(
+        x.data_ptr(), M, dp, w1.data_ptr(), b1.data_ptr(), w2.data_ptr(), b2.data_ptr(),
+        w3.data_ptr(), b3.data_ptr(), H, N, path, cols.data_ptr(), _stream_ptr(stream)))
+    return cols
 
 
 def gemm_bf16(a_bits, b_bits):

@@ -26,10 +26,13 @@
 #include <mutex>
 
 #include "gemm_tc.h"
+#include "tc_common.cuh"
 
 namespace rte {
 
 namespace {
+
+using namespace tc;
 
 constexpr int BM = 128, BK = 64;
 constexpr int A_BYTES = BM * BK * 2;  // one 128 x 64 chunk of A
@@ -64,100 +67,6 @@ constexpr int STAGE_BYTES = kEpiWarps * 32 * kStageLd * 4;
 constexpr int SMEM_BYTES = RING_BYTES + STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int kProducerWarp = kEpiWarps, kMmaWarp = kEpiWarps + 1;
 constexpr int kThreads = 32 * (kEpiWarps + 2);
-constexpr long long kWaitLimit = 1ll << 24;  // try_wait rounds before giving up (~seconds)
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart (stride byte offset), leading byte offset unused (1),
-// descriptor version 1 (bits 46-47), layout type 2 = SWIZZLE_128B (61-63).
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
-  d |= (uint64_t)1 << 16;
-  d |= (uint64_t)(1024 >> 4) << 32;
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
-  return d;
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait; returns false (and records `code`) when the limit runs out
-// or another role of the CTA has raised *abort.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code,
-                                          const int* abort = nullptr) {
-  for (long long i = 0; i < kWaitLimit; ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (abort && (i & 1023) == 1023 && *(volatile const int*)abort) return false;
-  }
-  if (err) atomicCAS(err, 0, code);
-  return false;
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
-                                            uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-               : "memory");
-}
-
-// 32 consecutive accumulator columns of this thread's TMEM lane; the caller
-// waits with tmem_wait_ld before reading r.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
-      "%30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
-        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
-        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-}
-
-__device__ __forceinline__ void tmem_wait_ld() {
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
 
 template <int BN_>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -480,6 +389,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
+}  // namespace
+
+namespace tc {
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point, so the
 // library needs no link-time dependency on libcuda.
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
@@ -487,7 +400,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-EncodeTiledFn encoder() {
+static EncodeTiledFn encoder() {
   static EncodeTiledFn fn = nullptr;
   static std::once_flag once;
   std::call_once(once, [] {
@@ -501,21 +414,22 @@ EncodeTiledFn encoder() {
   return fn;
 }
 
-bool make_map(CUtensorMap* m, const void* base, int rows, int K, int box_rows) {
+bool make_map_bf16(CUtensorMap* m, const void* base, int rows, int K, int box_k, int box_rows) {
   EncodeTiledFn enc = encoder();
   if (!enc) return false;
   cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)K * 2};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-}  // namespace
+}  // namespace tc
 
 cudaError_t gemm_bf16_tn(const GemmArgs& g, cudaStream_t st) {
+  using namespace tc;
   if (g.M <= 0 || g.N <= 0 || g.K <= 0 || (g.K & 7) || !g.A || !g.B) return cudaErrorInvalidValue;
   if (((uintptr_t)g.A & 15) || ((uintptr_t)g.B & 15)) return cudaErrorInvalidValue;
   if (g.epilogue != kEpiBiasArgmax && !g.C) return cudaErrorInvalidValue;
@@ -528,7 +442,7 @@ cudaError_t gemm_bf16_tn(const GemmArgs& g, cudaStream_t st) {
   const bool wide = g.epilogue == kEpiBiasArgmax && g.N >= 1024;
   const int bn = wide ? 256 : 128;
   CUtensorMap ma, mb;
-  if (!make_map(&ma, g.A, g.M, g.K, BM) || !make_map(&mb, g.B, g.N, g.K, bn))
+  if (!make_map_bf16(&ma, g.A, g.M, g.K, BK, BM) || !make_map_bf16(&mb, g.B, g.N, g.K, BK, bn))
     return cudaErrorNotSupported;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;

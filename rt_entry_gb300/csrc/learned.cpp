@@ -10,6 +10,7 @@
 
 #include "gemm_tc.h"
 #include "index_impl.h"
+#include "mlp_head.h"
 #include "mlp_kernels.h"
 #include "rtentry.h"
 
@@ -153,22 +154,51 @@ cudaError_t gemm(const void* A, const void* B, int M, int N, int K, int epi, voi
 
 int round8(int v) { return (v + 7) & ~7; }
 
+// The head's forward pass on zeroed keys: the fused kernel (path 0,
+// mlp_head.cu) or the three layer-by-layer GEMMs (path 1).  Both round the
+// hidden activations to BF16 the same way and give the same keys.
+rte_status head_keys(const MlpHeadArgs& h, int path, cudaStream_t st) {
+  if (path == 0) {
+    if (!mlp_head_supported(h)) return fail(RTE_EINVAL, "shape not supported by the fused head kernel");
+    RTE_CUDA(mlp_head_argmax(h, st));
+    return RTE_OK;
+  }
+  AsyncBuf h1, h2;
+  RTE_CUDA(h1.alloc((size_t)h.M * h.H * 2, st));
+  RTE_CUDA(h2.alloc((size_t)h.M * h.H * 2, st));
+  RTE_CUDA(gemm(h.X, h.W1, h.M, h.H, h.dp, kEpiBiasReluBF16, h1.p, h.H, h.b1, nullptr, h.err, st));
+  RTE_CUDA(gemm(h1.p, h.W2, h.M, h.H, h.H, kEpiBiasReluBF16, h2.p, h.H, h.b2, nullptr, h.err, st));
+  RTE_CUDA(gemm(h2.p, h.W3, h.M, h.N, h.H, kEpiBiasArgmax, nullptr, 0, h.b3, h.keys, h.err, st));
+  return RTE_OK;
+}
+
 // MLP forward for nq rows of X (BF16 [nq x dp]) -> packed argmax key per row
-// (keys [nq], zeroed here unless keys_zeroed).
+// (keys [nq], zeroed here unless keys_zeroed).  The fused kernel where it
+// takes the shape, the layer-by-layer GEMMs otherwise.
 rte_status mlp_keys_bf16(const rte_index* x, const uint16_t* X, int64_t nq, unsigned long long* keys,
                          int* d_err, cudaStream_t st, bool keys_zeroed) {
   const Mlp& m = x->mlp;
-  AsyncBuf h1, h2;
-  RTE_CUDA(h1.alloc((size_t)nq * m.hidden * 2, st));
-  RTE_CUDA(h2.alloc((size_t)nq * m.hidden * 2, st));
   if (!keys_zeroed) RTE_CUDA(cudaMemsetAsync(keys, 0, (size_t)nq * 8, st));
-  RTE_CUDA(gemm(X, m.W16[0].p, (int)nq, m.hidden, m.dp, kEpiBiasReluBF16, h1.p, m.hidden, m.b[0].p,
-                nullptr, d_err, st));
-  RTE_CUDA(gemm(h1.p, m.W16[1].p, (int)nq, m.hidden, m.hidden, kEpiBiasReluBF16, h2.p, m.hidden,
-                m.b[1].p, nullptr, d_err, st));
-  RTE_CUDA(gemm(h2.p, m.W16[2].p, (int)nq, m.classes, m.hidden, kEpiBiasArgmax, nullptr, 0,
-                m.b[2].p, keys, d_err, st));
-  return RTE_OK;
+  MlpHeadArgs h{};
+  h.X = X;
+  h.W1 = m.W16[0].p;
+  h.W2 = m.W16[1].p;
+  h.W3 = m.W16[2].p;
+  h.b1 = m.b[0].p;
+  h.b2 = m.b[1].p;
+  h.b3 = m.b[2].p;
+  h.M = (int)nq;
+  h.dp = m.dp;
+  h.H = m.hidden;
+  h.N = m.classes;
+  h.keys = keys;
+  h.err = d_err;
+  if (mlp_head_supported(h)) {
+    const cudaError_t e = mlp_head_argmax(h, st);
+    if (e == cudaSuccess) return RTE_OK;
+    if (e != cudaErrorNotSupported) RTE_CUDA(e);  // NotSupported: nothing was launched
+  }
+  return head_keys(h, 1, st);
 }
 
 // MLP forward for nq rows of X (BF16 [nq x dp]) -> class (subtree) per row.
@@ -280,6 +310,48 @@ rte_status fwd_bwd(const Mlp& m, const uint16_t* Xb, const int32_t* yb, int M, S
 }
 
 }  // namespace
+
+extern "C" rte_status rte_mlp_head_argmax(const uint16_t* X, int M, int dp, const uint16_t* W1,
+                                          const float* b1, const uint16_t* W2, const float* b2,
+                                          const uint16_t* W3, const float* b3, int H, int N, int path,
+                                          int32_t* cols, void* stream) {
+  clear_error();
+  if (!X || !W1 || !b1 || !W2 || !b2 || !W3 || !b3 || !cols || M <= 0 || dp <= 0 || H <= 0 || N <= 0)
+    return fail(RTE_EINVAL, "bad head arguments");
+  if (path != 0 && path != 1) return fail(RTE_EINVAL, "path must be 0 (fused) or 1 (layer by layer)");
+  if (dp % 8 || H % 8) return fail(RTE_EINVAL, "dp and H must be multiples of 8");
+  const void* ptrs[] = {X, W1, b1, W2, b2, W3, b3, cols};
+  for (const void* q : ptrs)
+    if (!is_device_ptr(q)) return fail(RTE_EINVAL, "rte_mlp_head_argmax takes device pointers");
+  cudaStream_t st = (cudaStream_t)stream;
+  AsyncBuf keys, e;
+  RTE_CUDA(keys.alloc((size_t)M * 8, st));
+  RTE_CUDA(cudaMemsetAsync(keys.p, 0, (size_t)M * 8, st));
+  RTE_CUDA(e.alloc(4, st));
+  RTE_CUDA(cudaMemsetAsync(e.p, 0, 4, st));
+  MlpHeadArgs h{};
+  h.X = X;
+  h.W1 = W1;
+  h.W2 = W2;
+  h.W3 = W3;
+  h.b1 = b1;
+  h.b2 = b2;
+  h.b3 = b3;
+  h.M = M;
+  h.dp = dp;
+  h.H = H;
+  h.N = N;
+  h.keys = keys.as<unsigned long long>();
+  h.err = e.as<int>();
+  rte_status s = head_keys(h, path, st);
+  if (s != RTE_OK) return s;
+  RTE_CUDA(launch_argmax_to_leaf(keys.as<unsigned long long>(), M, nullptr, cols, st));
+  int herr = 0;
+  RTE_CUDA(cudaMemcpyAsync(&herr, e.p, 4, cudaMemcpyDeviceToHost, st));
+  RTE_CUDA(cudaStreamSynchronize(st));
+  if (herr) return fail(RTE_ETIMEOUT, "head pipeline wait ran out (code " + std::to_string(herr) + ")");
+  return RTE_OK;
+}
 
 namespace rte {
 

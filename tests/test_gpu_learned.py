@@ -56,6 +56,45 @@ def test_tensor_core_bias_argmax_matches_fp64(lib, cuda):
     assert (cols < N // 2).all()
 
 
+def test_fused_head_equals_layer_by_layer(lib, cuda):
+    """The learned head in one kernel (h1, h2 kept in shared memory) against
+    the three layer-by-layer GEMMs: the same columns for every row, over
+    shapes with partial row blocks, a batch smaller than one block, narrow
+    and wide last layers, H = 64 .. 256 and inputs not a multiple of 64
+    wide.  The chosen column is also the FP64 maximum of the same BF16
+    network within the accumulation error of the last layer."""
+    import torch
+    import rt_entry_gb300 as r
+    g = torch.Generator(device="cpu").manual_seed(11)
+    for M, dp, H, N in [(10000, 128, 256, 4096), (3001, 96, 256, 1000), (77, 128, 128, 300),
+                        (1500, 256, 64, 100), (640, 40, 192, 2304)]:
+        x = torch.randn(M, dp, generator=g).mul(2).bfloat16().cuda()
+        w1 = torch.randn(H, dp, generator=g).mul(dp ** -0.5).bfloat16().cuda()
+        w2 = torch.randn(H, H, generator=g).mul(H ** -0.5).bfloat16().cuda()
+        w3 = torch.randn(N, H, generator=g).mul(H ** -0.5).bfloat16().cuda()
+        b1, b2, b3 = (torch.randn(n, generator=g).mul(0.1).cuda() for n in (H, H, N))
+        fused = r.mlp_head_argmax(x, w1, b1, w2, b2, w3, b3, path=0)
+        ref = r.mlp_head_argmax(x, w1, b1, w2, b2, w3, b3, path=1)
+        torch.cuda.synchronize()
+        assert torch.equal(fused, ref), (M, dp, H, N, int((fused != ref).sum()))
+        # FP64 check of the last layer on the GEMM path's own BF16 h2
+        h1 = torch.relu(x.double() @ w1.double().T + b1.double()).bfloat16().double()
+        h2 = torch.relu(h1 @ w2.double().T + b2.double()).bfloat16().double()
+        logits = h2 @ w3.double().T + b3.double()
+        best = logits.max(1).values
+        got = logits.gather(1, fused.long()[:, None])[:, 0]
+        # rows whose BF16 h2 differs from the FP64-rounded one are excluded
+        # by the tolerance only where rounding flips change the maximum
+        frac = ((best - got) <= 1e-4 * logits.abs().max()).double().mean().item()
+        assert frac > 0.99, (M, dp, H, N, frac)
+    with pytest.raises(RuntimeError):  # H not a multiple of 64: the fused form refuses it
+        x = torch.zeros(128, 64, dtype=torch.bfloat16, device="cuda")
+        w = torch.zeros(72, 64, dtype=torch.bfloat16, device="cuda")
+        w2 = torch.zeros(72, 72, dtype=torch.bfloat16, device="cuda")
+        b = torch.zeros(72, device="cuda")
+        r.mlp_head_argmax(x, w, b, w2, b, w2, b, path=0)
+
+
 def test_mlp_gradients_match_oracle(lib, cuda):
     import rt_entry_gb300 as r
     from oracle import mlp_ref
