@@ -208,12 +208,13 @@ def truncated_pca_bench(w, r, ds, torch, stream, flush, dev, keep=64, steps=5):
                     "of the final pool against the original rows"}
 
 
-def stream_bench(idx, r, ds, torch, stream, n_batches=2000, max_batch=8192):
+def stream_bench(idx, r, ds, torch, stream, entry_mode, n_batches=2000, max_batch=8192):
     """Config 5: uneven batches (sizes floor(exp(U[0, ln 8192])), k in
     {1, 10, 100}) over the config-2 index.  Per k: parameters autotuned for
     recall@k >= 0.95 on 2000 held-out queries, then one CUDA-graph batcher
     (capacity 8192) replays the whole query path for every batch.  Latency is
-    wall time per batch: pinned host queries in, host results out."""
+    wall time per batch: pinned host queries in, host results out.
+    entry_mode: learned entries (the head in the graph) or kd-tree entries."""
     mix = ds.mixture_config(2)
     pool = mix.sample(65536, ds.SEED_STREAM)
     tune_q = mix.sample(2000, ds.SEED_STREAM + 1)
@@ -223,7 +224,7 @@ def stream_bench(idx, r, ds, torch, stream, n_batches=2000, max_batch=8192):
     batchers, tuned = {}, {}
     for k in sorted(set(int(x) for x in ks)):
         p, rep = idx.autotune(tune_q, tune_gt, k=k, target_recall=RECALL_TARGET,
-                              precision=r.PREC_BF16, rerank=1)
+                              precision=r.PREC_BF16, rerank=1, entry_mode=entry_mode)
         batchers[k] = idx.batcher(max_batch, params=p)
         tuned[k] = {"beam": p.beam, "search_width": p.search_width, "bloom_words": p.bloom_words,
                     "warps_per_block": p.warps_per_block, **{kk: rep[kk] for kk in ("recall", "met_target")}}
@@ -251,7 +252,8 @@ def stream_bench(idx, r, ds, torch, stream, n_batches=2000, max_batch=8192):
     return {"batches": n_batches, "queries": total, "qps": total / wall,
             "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
             "tuned": {str(k): v for k, v in tuned.items()},
-            "path": "rte_batcher (one CUDA graph per k), BF16 distances + FP32 rerank, kd-tree entries"}
+            "path": "rte_batcher (one CUDA graph per k), BF16 distances + FP32 rerank, "
+                    + ("learned entries" if entry_mode == r.ENTRY_LEARNED else "kd-tree entries")}
 
 
 def main():
@@ -442,10 +444,12 @@ def main():
                          f"OpenMP over queries"}
         assert np.array_equal(oids, plain_ids), "GPU result differs from the oracle"
 
-    stream_res = None
+    stream_res = stream_kd = None
     if rank == 0 and not args.no_stream:
-        stream_res = stream_bench(idx, r, ds, torch, stream)
+        stream_res = stream_bench(idx, r, ds, torch, stream, r.ENTRY_LEARNED)
         log(f"stream {stream_res}")
+        stream_kd = stream_bench(idx, r, ds, torch, stream, r.ENTRY_KDTREE)
+        log(f"stream (kd-tree entries) {stream_kd}")
     # kd-tree entries from several containing leaves (the reference's
     # disabled multi-hit entry), FP32: informational
     multi_res = []
@@ -481,6 +485,7 @@ def main():
                               "recall_at_10": round(plain_recall, 4), "sweep": plain_sweep,
                               "speedup_of_headline": value / plain_qps},
                "stream": stream_res,
+               "stream_kdtree": stream_kd,
                "truncated_pca": trunc_res,
                "multi_leaf_kdtree": multi_res or None,
                "roofline": roof_plain,

@@ -172,7 +172,10 @@ rte_status rte_search_projected_noalloc(rte_index* idx, const float* projected,
  * A batcher captures the whole query path (projection, kd-tree location,
  * persistent search) once into a CUDA graph sized for max_nq queries; the
  * kernels read the batch size from device memory, so every batch of up to
- * max_nq queries replays the same graph.  Random or kd-tree entries. */
+ * max_nq queries replays the same graph.  Random, kd-tree or learned
+ * entries; learned entries need a PCA index whose trained head the fused
+ * head kernel takes (RTE_EINVAL otherwise) and give the same results as
+ * rte_search's learned path. */
 typedef struct rte_batcher rte_batcher;
 rte_status rte_batcher_create(rte_index* idx, int64_t max_nq, const rte_search_params* params,
                               rte_batcher** out);
@@ -305,7 +308,8 @@ rte_status rte_gemm_bf16(const uint16_t* A, const uint16_t* B, int M, int N, int
 /* The learned head's last layer alone: for each row m, the column n of the
  * largest A[m]·B[n] + bias[n] (the first one on ties), through the same
  * tensor-core kernel and fused argmax epilogue as rte_learned_predict.
- * Host or device pointers; cols [M] int32.  (No reference counterpart.) */
+ * Host or device pointers; cols [M] int32, -1 for a row whose logits are
+ * all NaN.  (No reference counterpart.) */
 rte_status rte_gemm_bf16_bias_argmax(const uint16_t* A, const uint16_t* B, const float* bias, int M,
                                      int N, int K, int32_t* cols, void* stream);
 
@@ -316,7 +320,7 @@ rte_status rte_gemm_bf16_bias_argmax(const uint16_t* A, const uint16_t* B, const
  * path 0: the fused single-kernel form rte_search uses (H a multiple of 64
  * up to 256, dp up to 256; RTE_EINVAL otherwise); path 1: the three
  * layer-by-layer GEMMs.  Both give the same columns.  Device pointers;
- * cols [M] int32.  RTE_ETIMEOUT if a bounded pipeline wait ran out.  (No
+ * cols [M] int32, -1 for a row whose logits are all NaN.  RTE_ETIMEOUT if a bounded pipeline wait ran out.  (No
  * reference counterpart.) */
 rte_status rte_mlp_head_argmax(const uint16_t* X, int M, int dp, const uint16_t* W1, const float* b1,
                                const uint16_t* W2, const float* b2, const uint16_t* W3, const float* b3,

@@ -458,11 +458,16 @@ __global__ void locate_in_subtree_wide(const WideNode* __restrict__ wide,
                                        const float* __restrict__ pts, int64_t n, int stride,
                                        const unsigned long long* __restrict__ keys,
                                        const int32_t* __restrict__ start_ref,
-                                       const int32_t* __restrict__ fallback_leaf,
-                                       int32_t* __restrict__ out) {
+                                       const int32_t* __restrict__ fallback_leaf, int n_classes,
+                                       const int* __restrict__ n_dev, int32_t* __restrict__ out) {
+  if (n_dev) n = min(n, (int64_t)*n_dev);  // graph replay: points beyond the batch are idle
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int c = 0x7fffffff - (int)(keys[i] & 0xffffffffu);
+  if (c < 0 || c >= n_classes) {  // no key (the head wrote none): leaf 0, as on a miss
+    out[i] = 0;
+    return;
+  }
   float x, y, z;
   load_xyz(pts, i, stride, x, y, z);
   int stack[kLocStack];
@@ -488,12 +493,16 @@ __global__ void locate_in_subtree(const BvhNode* __restrict__ nodes, const float
                                   int64_t n, int stride, const int32_t* __restrict__ cls,
                                   const unsigned long long* __restrict__ keys,
                                   const int32_t* __restrict__ start_node,
-                                  const int32_t* __restrict__ fallback_leaf,
+                                  const int32_t* __restrict__ fallback_leaf, int n_classes,
                                   int32_t* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   // the class is given, or decoded from the packed argmax key (gemm_tc.h)
   const int c = keys ? 0x7fffffff - (int)(keys[i] & 0xffffffffu) : cls[i];
+  if (c < 0 || c >= n_classes) {  // no key (the head wrote none): leaf 0, as on a miss
+    out[i] = 0;
+    return;
+  }
   float x, y, z;
   load_xyz(pts, i, stride, x, y, z);
   int stack[kBvhMaxDepth];
@@ -539,11 +548,11 @@ __global__ void bf16_norms(const uint16_t* __restrict__ il16, int64_t n, int C,
 cudaError_t launch_locate_in_subtree(const BvhNode* nodes, const float* pts, int64_t n, int stride,
                                      const int32_t* cls, const unsigned long long* keys,
                                      const int32_t* start_node, const int32_t* fallback_leaf,
-                                     int32_t* out, cudaStream_t st) {
+                                     int n_classes, int32_t* out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   if (!cls == !keys) return cudaErrorInvalidValue;
   locate_in_subtree<<<(unsigned)((n + 63) / 64), 64, 0, st>>>(nodes, pts, n, stride, cls, keys,
-                                                                start_node, fallback_leaf, out);
+                                                                start_node, fallback_leaf, n_classes, out);
   return cudaGetLastError();
 }
 
@@ -597,6 +606,18 @@ cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, in
   return cudaGetLastError();
 }
 
+cudaError_t launch_project_bf16_dyn(const float* x, int64_t cap, const int* n_dev, int d, int xstride,
+                                    const float* mean, const float* V, int vstride, int k, float* out,
+                                    int ostride, void* out16, float s16, int ld16, uint32_t* zero,
+                                    int64_t zero_words, cudaStream_t st) {
+  if (ld16 < k || ld16 > ((k + kPrCols - 1) / kPrCols) * kPrCols) return cudaErrorInvalidValue;
+  dim3 grid((unsigned)((cap + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
+  project_rows<true><<<grid, kPrThreads, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride, n_dev,
+                                                  reinterpret_cast<__nv_bfloat16*>(out16), s16, ld16, zero,
+                                                  zero_words);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_interleave(const float* src, int64_t n, int d, int C, float* il32,
                               void* il16, uint8_t* il8, float* scale8, float* xyz,
                               cudaStream_t st) {
@@ -633,10 +654,12 @@ cudaError_t launch_dequant(const void* il, const float* scale8, int precision, i
 cudaError_t launch_locate_in_subtree_wide(const WideNode* wide, const float* pts, int64_t n,
                                           int stride, const unsigned long long* keys,
                                           const int32_t* start_ref, const int32_t* fallback_leaf,
-                                          int32_t* out, cudaStream_t st) {
+                                          int n_classes, int32_t* out, cudaStream_t st,
+                                          const int* n_dev) {
   if (n == 0) return cudaSuccess;
   locate_in_subtree_wide<<<(unsigned)((n + 63) / 64), 64, 0, st>>>(wide, pts, n, stride, keys,
-                                                                     start_ref, fallback_leaf, out);
+                                                                     start_ref, fallback_leaf, n_classes,
+                                                                     n_dev, out);
   return cudaGetLastError();
 }
 
@@ -658,8 +681,11 @@ cudaError_t launch_locate(const WideNode* wide, int n_wide, const float* pts, in
 }
 
 cudaError_t launch_locate_dyn(const WideNode* wide, int n_wide, const float* pts, int64_t cap,
-                              const int* n_dev, int stride, int32_t* out, cudaStream_t st) {
-  locate_points<true><<<(unsigned)((cap + 63) / 64), 64, 0, st>>>(wide, n_wide, pts, cap, stride, out, n_dev);
+                              const int* n_dev, int stride, int32_t* out, cudaStream_t st, bool top_cache) {
+  if (top_cache)
+    locate_points<true><<<(unsigned)((cap + 63) / 64), 64, 0, st>>>(wide, n_wide, pts, cap, stride, out, n_dev);
+  else
+    locate_points<false><<<(unsigned)((cap + 63) / 64), 64, 0, st>>>(wide, n_wide, pts, cap, stride, out, n_dev);
   return cudaGetLastError();
 }
 

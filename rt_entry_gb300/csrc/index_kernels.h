@@ -56,8 +56,13 @@ cudaError_t launch_project_bf16(const float* x, int64_t n, int d, int xstride, c
 cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, int d, int xstride,
                                const float* mean, const float* V, int vstride, int k, float* out,
                                int ostride, cudaStream_t st);
+// launch_project_bf16 for graph replay, plus the zeroed word range.
+cudaError_t launch_project_bf16_dyn(const float* x, int64_t cap, const int* n_dev, int d, int xstride,
+                                    const float* mean, const float* V, int vstride, int k, float* out,
+                                    int ostride, void* out16, float s16, int ld16, uint32_t* zero,
+                                    int64_t zero_words, cudaStream_t st);
 cudaError_t launch_locate_dyn(const WideNode* wide, int n_wide, const float* pts, int64_t cap,
-                              const int* n_dev, int stride, int32_t* out, cudaStream_t st);
+                              const int* n_dev, int stride, int32_t* out, cudaStream_t st, bool top_cache = true);
 cudaError_t launch_interleave(const float* src, int64_t n, int d, int C, float* il32, void* il16,
                               uint8_t* il8, float* scale8, float* xyz, cudaStream_t st);
 cudaError_t launch_deinterleave(const float* il32, int64_t n, int d, int C, float* dst,
@@ -68,17 +73,20 @@ cudaError_t launch_bf16_norms(const uint16_t* il16, int64_t n, int C, float* out
 cudaError_t launch_dequant(const void* il, const float* scale8, int precision, int64_t n, int d,
                            int C, float* dst, cudaStream_t st);
 // The class of point i is cls[i], or decoded from the packed argmax key
-// keys[i] (exactly one of the two is given).
+// keys[i] (exactly one of the two is given).  A class outside [0, n_classes)
+// (a key the head never wrote) gives leaf 0, the miss rule's leaf.
 cudaError_t launch_locate_in_subtree(const BvhNode* nodes, const float* pts, int64_t n, int stride,
                                      const int32_t* cls, const unsigned long long* keys,
                                      const int32_t* start_node, const int32_t* fallback_leaf,
-                                     int32_t* out, cudaStream_t st);
+                                     int n_classes, int32_t* out, cudaStream_t st);
 // launch_locate_in_subtree on the 8-wide tree: the class of point i, decoded
-// from keys[i], starts at start_ref[class] (a wide node, or a leaf).
+// from keys[i], starts at start_ref[class] (a wide node, or a leaf).  n_dev:
+// the live point count for graph replay (grid sized for n).
 cudaError_t launch_locate_in_subtree_wide(const WideNode* wide, const float* pts, int64_t n,
                                           int stride, const unsigned long long* keys,
                                           const int32_t* start_ref, const int32_t* fallback_leaf,
-                                          int32_t* out, cudaStream_t st);
+                                          int n_classes, int32_t* out, cudaStream_t st,
+                                          const int* n_dev = nullptr);
 // The first H containing leaves per point ([n][H], -1 padded, leaf 0 first on
 // a miss).
 cudaError_t launch_locate_multi(const WideNode* wide, int n_wide, const float* pts, int64_t n,

@@ -388,11 +388,11 @@ rte_status learned_leaves(const rte_index* x, const float* d_proj, int64_t nq, i
   if (m.class_wide.p) {
     RTE_CUDA(launch_locate_in_subtree_wide(x->d_wide.p, d_proj, nq, x->search_dim,
                                            keys, m.class_wide.p,
-                                           m.class_leaf0.p, d_leaf, st));
+                                           m.class_leaf0.p, m.real_classes, d_leaf, st));
   } else {
     RTE_CUDA(launch_locate_in_subtree(x->d_nodes.p, d_proj, nq, x->search_dim, nullptr,
                                       keys, m.class_node.p,
-                                      m.class_leaf0.p, d_leaf, st));
+                                      m.class_leaf0.p, m.real_classes, d_leaf, st));
   }
   return RTE_OK;
 }

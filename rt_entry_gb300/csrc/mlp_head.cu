@@ -77,9 +77,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int H = g.H;
+  const int M = g.M_dev ? min(g.M, max(*g.M_dev, 0)) : g.M;  // rows of this launch
   const int nk1 = (g.dp + kBK - 1) / kBK, nkh = H / kBK;
   const int n3 = (g.N + BN3 - 1) / BN3;
-  const int m_tiles = (g.M + kBM - 1) / kBM;
+  const int m_tiles = (M + kBM - 1) / kBM;
   const long long total = (long long)m_tiles * n3;
   const long long t_begin = total * blockIdx.x / gridDim.x;
   const long long t_end = total * (blockIdx.x + 1) / gridDim.x;
@@ -290,7 +291,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           bb = best[j];
           bc = best_col[j];
         }
-      if (row < g.M && bc >= 0) atomicMax(g.keys + row, argmax_key(bb, bc));
+      if (row < M && bc >= 0) atomicMax(g.keys + row, argmax_key(bb, bc));
     };
     auto last = [&](int nt) -> bool {
       if (!wait_full()) return false;
@@ -359,6 +360,29 @@ bool mlp_head_supported(const MlpHeadArgs& a) {
          ((uintptr_t)a.W2 & 15) == 0 && ((uintptr_t)a.W3 & 15) == 0;
 }
 
+namespace {
+int g_num_sms[64] = {0};
+bool g_attr[2][64] = {{false}};
+}  // namespace
+
+cudaError_t mlp_head_prepare(int N) {
+  const bool wide = N >= 256;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!g_attr[wide][dev]) {
+    cudaError_t e = wide ? cudaFuncSetAttribute(mlp_head_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                kSmemBytes)
+                         : cudaFuncSetAttribute(mlp_head_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                kSmemBytes);
+    if (e != cudaSuccess) return e;
+    g_attr[wide][dev] = true;
+  }
+  if (g_num_sms[dev] == 0 &&
+      cudaDeviceGetAttribute(&g_num_sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    g_num_sms[dev] = 1;
+  return cudaSuccess;
+}
+
 cudaError_t mlp_head_argmax(const MlpHeadArgs& a, cudaStream_t st) {
   if (!mlp_head_supported(a)) return cudaErrorNotSupported;
   const bool wide = a.N >= 256;
@@ -367,21 +391,11 @@ cudaError_t mlp_head_argmax(const MlpHeadArgs& a, cudaStream_t st) {
   if (!make_map_bf16(&mx, a.X, a.M, a.dp, kBK, kBM) || !make_map_bf16(&m1, a.W1, a.H, a.dp, kBK, a.H) ||
       !make_map_bf16(&m2, a.W2, a.H, a.H, kBK, a.H) || !make_map_bf16(&m3, a.W3, a.N, a.H, kBK, bn3))
     return cudaErrorNotSupported;
+  cudaError_t pe = mlp_head_prepare(a.N);
+  if (pe != cudaSuccess) return pe;
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  static int num_sms[64] = {0};
-  static bool attr[2][64] = {{false}};
-  if (!attr[wide][dev]) {
-    cudaError_t e = wide ? cudaFuncSetAttribute(mlp_head_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                kSmemBytes)
-                         : cudaFuncSetAttribute(mlp_head_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                kSmemBytes);
-    if (e != cudaSuccess) return e;
-    attr[wide][dev] = true;
-  }
-  if (num_sms[dev] == 0 &&
-      cudaDeviceGetAttribute(&num_sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    num_sms[dev] = 1;
+  cudaGetDevice(&dev);
+  int* num_sms = g_num_sms;
   const long long tiles = (long long)((a.M + kBM - 1) / kBM) * ((a.N + bn3 - 1) / bn3);
   const dim3 grid((unsigned)(tiles < num_sms[dev] ? tiles : num_sms[dev]));
   if (wide)

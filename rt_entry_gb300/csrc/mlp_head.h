@@ -23,11 +23,19 @@ struct MlpHeadArgs {
   int M, dp, H, N;
   unsigned long long* keys;  // [M], zero on entry
   int* err;                  // device flag: a bounded wait ran out (non-zero code)
+  // graph replay: the live row count, read at run time (<= M; the grid and
+  // tensor maps are sized for M rows); null for a plain launch
+  const int* M_dev = nullptr;
 };
 
 // True when the fused kernel takes this shape: H a multiple of 64 up to 256,
 // dp a multiple of 8 up to 256, 16-byte aligned operands.
 bool mlp_head_supported(const MlpHeadArgs& a);
+
+// The launch attributes (shared-memory size) and the SM count for the
+// current device, set once; call it before capturing mlp_head_argmax into a
+// CUDA graph.
+cudaError_t mlp_head_prepare(int N);
 
 // cudaErrorNotSupported for shapes mlp_head_supported rejects (or when the
 // driver's tensor-map encoder is unavailable); the caller then runs the

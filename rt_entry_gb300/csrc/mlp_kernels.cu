@@ -129,10 +129,15 @@ __global__ void gather_rows_k(const __nv_bfloat16* __restrict__ src, int dp,
 }
 
 // argmax key -> class column; class -> leaf through class_leaf (null: identity).
+// A zero key (no column was a maximum: every logit NaN) gives -1.
 __global__ void argmax_to_leaf_k(const unsigned long long* __restrict__ keys, int n,
                                  const int32_t* __restrict__ class_leaf, int32_t* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (keys[i] == 0ull) {
+    out[i] = -1;
+    return;
+  }
   const int col = 0x7fffffff - (int)(keys[i] & 0xffffffffu);
   out[i] = class_leaf ? class_leaf[col] : col;
 }

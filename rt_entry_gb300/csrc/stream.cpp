@@ -8,7 +8,11 @@
 // search) captured once into a CUDA graph for batches of up to max_nq
 // queries.  The kernels read the batch size from device memory, so one
 // instantiated graph serves every batch size without re-capture; a batch
-// costs one graph launch plus the copies of its queries and results.
+// costs one graph launch plus the copies of its queries and results.  With
+// learned entries the graph holds the same five kernels as rte_search's
+// learned path: the projection (with the head's BF16 input and the zeroed
+// keys / counters), the fused head and the subtree location on the main
+// branch, the kd-tree location on a parallel branch, then the search.
 //
 // rte_autotune: measures every candidate (beam, search width, bloom filter
 // size, warps per block) on a sample of queries with known neighbours and
@@ -21,6 +25,7 @@
 
 #include "index_impl.h"
 #include "index_kernels.h"
+#include "mlp_head.h"
 #include "rtentry.h"
 #include "search_dispatch.h"
 
@@ -36,17 +41,25 @@ struct rte_batcher {
   rte_search_params prm{};
   int64_t cap = 0;
   int k = 0;
-  cudaStream_t cap_stream = nullptr;
+  cudaStream_t cap_stream = nullptr, side_stream = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   DevBuf<float> dq, dproj, ddist;
-  DevBuf<int32_t> dhits, dids, dn;
+  DevBuf<int32_t> dhits, dhits2, dids, dn;
   DevBuf<unsigned int> dwork;
+  // learned entries: the head's BF16 input, and [keys (2 words a row) | error
+  // flag | work counter], zeroed by the projection
+  DevBuf<uint16_t> dxb;
+  DevBuf<uint32_t> dzero;
   int* hn = nullptr;  // pinned batch-size slot
   ~rte_batcher() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     if (cap_stream) cudaStreamDestroy(cap_stream);
+    if (side_stream) cudaStreamDestroy(side_stream);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
     if (hn) cudaFreeHost(hn);
   }
 };
@@ -62,16 +75,69 @@ rte_status capture(rte_batcher* b) {
   b->k = k;
   RTE_CUDA(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
   cudaStream_t st = b->cap_stream;
-  RTE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  cudaError_t e = cudaMemsetAsync(b->dwork.p, 0, sizeof(unsigned int), st);
-  const float* qp = b->dq.p;
-  if (e == cudaSuccess && x->has_pca) {
-    e = launch_project_dyn(b->dq.p, b->cap, b->dn.p, x->dim, x->dim, x->d_mean.p, x->d_rot.p,
-                           x->search_dim, x->search_dim, b->dproj.p, x->search_dim, st);
-    qp = b->dproj.p;
+  const bool learned = b->prm.entry_mode == RTE_ENTRY_LEARNED;
+  if (learned) {
+    RTE_CUDA(mlp_head_prepare(x->mlp.classes));  // no attribute calls inside the capture
+    RTE_CUDA(cudaStreamCreateWithFlags(&b->side_stream, cudaStreamNonBlocking));
+    RTE_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    RTE_CUDA(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
   }
-  if (e == cudaSuccess && b->prm.entry_mode == RTE_ENTRY_KDTREE)
-    e = launch_locate_dyn(x->d_wide.p, (int)x->d_wide.n, qp, b->cap, b->dn.p, x->search_dim, b->dhits.p, st);
+  RTE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  const float* qp = b->dq.p;
+  unsigned int* work = b->dwork.p;
+  unsigned long long* keys = nullptr;
+  if (learned) {
+    // projection + head input + zeroed keys, error flag and work counter
+    const int64_t zwords = b->cap * 2 + 2;
+    keys = reinterpret_cast<unsigned long long*>(b->dzero.p);
+    work = b->dzero.p + b->cap * 2 + 1;
+    e = launch_project_bf16_dyn(b->dq.p, b->cap, b->dn.p, x->dim, x->dim, x->d_mean.p, x->d_rot.p,
+                                x->search_dim, x->search_dim, b->dproj.p, x->search_dim, b->dxb.p,
+                                x->mlp.in_scale, x->mlp.dp, b->dzero.p, zwords, st);
+    qp = b->dproj.p;
+    // the kd-tree leaf on a parallel branch
+    if (e == cudaSuccess) e = cudaEventRecord(b->fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side_stream, b->fork, 0);
+    if (e == cudaSuccess)
+      e = launch_locate_dyn(x->d_wide.p, (int)x->d_wide.n, qp, b->cap, b->dn.p, x->search_dim, b->dhits2.p,
+                            b->side_stream, /*top_cache=*/false);
+    if (e == cudaSuccess) e = cudaEventRecord(b->join, b->side_stream);
+    if (e == cudaSuccess) {
+      const Mlp& m = x->mlp;
+      MlpHeadArgs h{};
+      h.X = b->dxb.p;
+      h.W1 = m.W16[0].p;
+      h.W2 = m.W16[1].p;
+      h.W3 = m.W16[2].p;
+      h.b1 = m.b[0].p;
+      h.b2 = m.b[1].p;
+      h.b3 = m.b[2].p;
+      h.M = (int)b->cap;
+      h.dp = m.dp;
+      h.H = m.hidden;
+      h.N = m.classes;
+      h.keys = keys;
+      h.err = reinterpret_cast<int*>(b->dzero.p + b->cap * 2);
+      h.M_dev = b->dn.p;
+      e = mlp_head_argmax(h, st);
+    }
+    if (e == cudaSuccess)
+      e = launch_locate_in_subtree_wide(x->d_wide.p, qp, b->cap, x->search_dim, keys, x->mlp.class_wide.p,
+                                        x->mlp.class_leaf0.p, x->mlp.real_classes, b->dhits.p, st, b->dn.p);
+    // the join also ends the side branch inside the capture
+    cudaError_t ej = cudaStreamWaitEvent(st, b->join, 0);
+    if (e == cudaSuccess) e = ej;
+  } else {
+    e = cudaMemsetAsync(b->dwork.p, 0, sizeof(unsigned int), st);
+    if (e == cudaSuccess && x->has_pca) {
+      e = launch_project_dyn(b->dq.p, b->cap, b->dn.p, x->dim, x->dim, x->d_mean.p, x->d_rot.p,
+                             x->search_dim, x->search_dim, b->dproj.p, x->search_dim, st);
+      qp = b->dproj.p;
+    }
+    if (e == cudaSuccess && b->prm.entry_mode == RTE_ENTRY_KDTREE)
+      e = launch_locate_dyn(x->d_wide.p, (int)x->d_wide.n, qp, b->cap, b->dn.p, x->search_dim, b->dhits.p, st);
+  }
   if (e == cudaSuccess) {
     SearchArgs a{};
     a.base = x->il32.p;
@@ -83,9 +149,10 @@ rte_status capture(rte_batcher* b) {
     a.graph = x->graph.p;
     a.leaf_pids = x->has_kdtree ? x->d_pids.p : nullptr;
     a.hits = b->dhits.p;
+    a.hits2 = learned ? b->dhits2.p : nullptr;
     a.out_ids = b->dids.p;
     a.out_dists = b->ddist.p;
-    a.work = b->dwork.p;
+    a.work = work;
     a.np = (int)x->np;
     a.d = x->search_dim;
     a.qstride = x->search_dim;
@@ -119,8 +186,22 @@ extern "C" rte_status rte_batcher_create(rte_index* x, int64_t max_nq,
   if (!x || !params || !out) return fail(RTE_EINVAL, "NULL argument");
   *out = nullptr;
   if (max_nq <= 0 || max_nq >= INT32_MAX) return fail(RTE_EINVAL, "max_nq must be in [1, 2^31)");
-  if (params->entry_mode == RTE_ENTRY_LEARNED)
-    return fail(RTE_EINVAL, "the batcher serves random and kd-tree entries");
+  if (params->entry_mode == RTE_ENTRY_LEARNED) {
+    const Mlp& m = x->mlp;
+    if (!m.trained) return fail(RTE_ESTATE, "learned entries requested before rte_learned_train");
+    MlpHeadArgs h{};
+    h.X = h.W1 = h.W2 = h.W3 = m.W16[0].p;  // alignment of the model's own buffers
+    h.b1 = h.b2 = h.b3 = m.b[0].p;
+    h.keys = reinterpret_cast<unsigned long long*>(1);
+    h.M = 1;
+    h.dp = m.dp;
+    h.H = m.hidden;
+    h.N = m.classes;
+    if (!x->has_pca || !x->has_kdtree || m.d_in != x->search_dim || !m.class_wide.p ||
+        !mlp_head_supported(h))
+      return fail(RTE_EINVAL, "the batcher's learned path needs a PCA index, the 8-wide kd-tree classes "
+                              "and a head the fused kernel takes");
+  }
   if (params->rerank == 2) return fail(RTE_EINVAL, "the batcher does not rerank against the original rows");
   if (params->max_hits > 1) return fail(RTE_EINVAL, "the batcher locates one leaf per query");
   DeviceGuard guard(x->device);
@@ -138,6 +219,10 @@ extern "C" rte_status rte_batcher_create(rte_index* x, int64_t max_nq,
       b->dhits.alloc(max_nq) != cudaSuccess || b->dids.alloc((size_t)max_nq * kmax) != cudaSuccess ||
       b->ddist.alloc((size_t)max_nq * kmax) != cudaSuccess || b->dn.alloc(1) != cudaSuccess ||
       b->dwork.alloc(1) != cudaSuccess || cudaMallocHost(&b->hn, sizeof(int)) != cudaSuccess)
+    return bail(fail(RTE_ENOMEM, "batcher buffers"));
+  if (params->entry_mode == RTE_ENTRY_LEARNED &&
+      (b->dhits2.alloc(max_nq) != cudaSuccess || b->dxb.alloc((size_t)max_nq * x->mlp.dp) != cudaSuccess ||
+       b->dzero.alloc((size_t)max_nq * 2 + 2) != cudaSuccess))
     return bail(fail(RTE_ENOMEM, "batcher buffers"));
   rte_status s = capture(b);
   if (s != RTE_OK) return bail(s);

@@ -38,6 +38,32 @@ def test_batcher_equals_direct_search_for_every_batch_size(lib, cuda, prec):
     b.close()
 
 
+def test_learned_batcher_equals_direct_search(lib, cuda):
+    """Learned entries through the CUDA graph (projection with the head's
+    input, fused head, subtree location, kd-tree location on a parallel
+    branch, search) against rte_search's learned path, batch by batch: the
+    head's tile split and every kernel read the live batch size from device
+    memory."""
+    import torch
+
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    idx, base, q = _index()
+    idx.train_learned(ds.mixture_config(2).sample(20000, 77))
+    for beam, prec in [(16, 1), (32, 0)]:
+        p = r.default_params(beam=beam, k=10, precision=prec, rerank=int(prec > 0),
+                             entry_mode=r.ENTRY_LEARNED)
+        b = idx.batcher(1024, params=p)
+        qt = torch.from_numpy(q).cuda()
+        for s, e in [(0, 1), (1, 3), (3, 131), (131, 1024), (1024, 1500), (0, 7)]:
+            want, wd = idx.search(q[s:e], params=p)
+            ids, dd = b.search(q[s:e])
+            assert np.array_equal(ids, want) and np.array_equal(dd, wd), (beam, s, e)
+            ti, _ = b.search(qt[s:e])
+            assert np.array_equal(ti.cpu().numpy(), want), (beam, s, e)
+        b.close()
+
+
 def test_autotune_meets_the_recall_target(lib, cuda):
     import rt_entry_gb300 as r
     from rt_entry_gb300 import datasets as ds
