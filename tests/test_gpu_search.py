@@ -190,6 +190,28 @@ def test_locate_matches_oracle_including_faces(lib, orc, cuda):
     assert (want == 0).any()  # misses fall back to leaf 0
 
 
+def test_two_dimensional_space_locates_and_searches(lib, orc, cuda):
+    """A search space of fewer than three dimensions: the kd-tree is built on
+    the coordinates padded with zeros, and point location reads only the
+    coordinates the space has (the oracle is given the padded points)."""
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    rng = np.random.default_rng(21)
+    base = rng.uniform(0, 200, (3000, 2)).astype(np.float32)
+    q = rng.uniform(-10, 210, (400, 2)).astype(np.float32)
+    graph = ds.knn_graph(base, 32)
+    idx = r.Index.from_arrays(base, graph).build_kdtree(32, 0.2)
+    pad = lambda a: np.pad(a, ((0, 0), (0, 1)))
+    t, e, p = idx.kdtree()
+    b, pp = orc.kdtree_build(pad(idx.search_base()), 32)
+    assert np.array_equal(t, b) and np.array_equal(p, pp)
+    hits = orc.locate(e, pad(q))
+    assert np.array_equal(idx.locate(q), hits)
+    ids, dd = idx.search(q, beam=32, k=32)
+    oids, od = orc.search(idx.search_base(), q, graph, L=32, k=32, leaf_pids=p, hits=hits)
+    assert np.array_equal(ids, oids) and np.array_equal(dd, od)
+
+
 @pytest.mark.parametrize("L", [64, 16])
 @pytest.mark.parametrize("prec", [1, 2])
 @pytest.mark.parametrize("rerank", [0, 1])
