@@ -180,7 +180,10 @@ def _ptr(x):
 def _as(x, np_dtype, torch_dtype_name):
     if _is_torch(x):
         import torch
-        return x.to(getattr(torch, torch_dtype_name)).contiguous()
+        dt = getattr(torch, torch_dtype_name)
+        if x.dtype != dt:  # skips the dispatcher when nothing is to be done
+            x = x.to(dt)
+        return x if x.is_contiguous() else x.contiguous()
     return np.ascontiguousarray(x, dtype=np_dtype)
 
 
