@@ -166,7 +166,7 @@ rte_status rte_search_projected_noalloc(rte_index* idx, const float* projected,
                                         const rte_search_params* params, int32_t* out_ids,
                                         float* out_dists, void* stream);
 
-/* ---- uneven query streams (spec form 2; no reference counterpart:
+/* ---- uneven query streams (no reference counterpart:
  * the reference launches each stage separately and synchronises the device
  * after each, graph.cu:254-337) ----
  * A batcher captures the whole query path (projection, kd-tree location,
@@ -248,7 +248,7 @@ rte_status rte_kdtree_build_host(const float* xyz, int64_t n, int leaf_size, flo
  * column j, largest-magnitude component positive. */
 rte_status rte_sym_eig_host(const double* a, int n, double* w, double* v);
 
-/* ---- learned entry (no reference counterpart; spec form 4) ----
+/* ---- learned entry (no reference counterpart) ----
  * A 3-layer MLP (search-space query -> hidden -> hidden -> kd-tree subtree)
  * proposes the region of each query's entry; point location inside that
  * subtree picks the entry leaf.  With RTE_ENTRY_LEARNED the entry list

@@ -1,5 +1,5 @@
 // stream.cpp -- uneven query batches through one CUDA graph, and the
-// autotuner of the search parameters (spec form 2; the reference
+// autotuner of the search parameters (the reference
 // launches one kernel per stage with a device-wide synchronisation after
 // each, graph.cu:254-337, and its bloom autotune, auto_tune_bloom.h:71-89,
 // is computed but never used).
