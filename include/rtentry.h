@@ -139,7 +139,7 @@ rte_status rte_search(rte_index* idx, const float* queries, int64_t nq,
 
 /* Beam search from already projected queries [nq x search_dim].  hits [nq]
  * gives each query's leaf (NULL: run rte_locate first).  Used to feed
- * identical inputs to the search and to its checker. */
+ * identical inputs to the search and to the oracle. */
 rte_status rte_search_projected(rte_index* idx, const float* projected, const int32_t* hits,
                                 int64_t nq, const rte_search_params* params, int32_t* out_ids,
                                 float* out_dists, void* stream);

@@ -1,7 +1,7 @@
 """ORACLE -- CPU restatement of rt_entry's query path (test infrastructure).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
-leg may import this package.  It is the checker, never the thing measured or
+leg may import this package.  It is the oracle, never the thing measured or
 shipped: the product (``rt_entry_gb300``) has no dependency on it.
 
 ``build()`` compiles ``search_ref.cpp`` and ``kdtree_ref.cpp`` (plain C++,
@@ -54,7 +54,7 @@ def build(force: bool = False) -> str:
 
 
 def build_ref_launcher(force: bool = False) -> str | None:
-    """Driver-API launcher for the reference kernel cubins (GPU machine)."""
+    """Driver-API launcher for the reference kernel cubins (run on a GPU)."""
     src = os.path.join(HERE, "ref_launch.cpp")
     if not os.path.exists(src):
         return None
