@@ -59,12 +59,19 @@ struct Bloom {
   int lw;               // log2(words)
   int nh;
   // set_bit / test_bit: word x % SIZE, bit x / SIZE (graph_search.cuh:7-28).
-  // The loops are unrolled to the largest hash count (10), so each hash's
-  // multipliers are constant-bank operands.
+  // The first kUnrolled hashes are unrolled, so their multipliers are
+  // constant-bank operands; further hashes (up to 10) run in a loop, which
+  // keeps the kernel's code small.
+  static constexpr int kUnrolled = 3;
   __device__ __forceinline__ void add(uint32_t x) const {
 #pragma unroll
-    for (int h = 0; h < 10; ++h) {
+    for (int h = 0; h < kUnrolled; ++h) {
       if (h >= nh) break;
+      uint32_t b = bloom_hash(h, x, bits_mask);
+      atomicOr(&w[b & words_mask], 1u << (b >> lw));
+    }
+#pragma unroll 1
+    for (int h = kUnrolled; h < nh; ++h) {
       uint32_t b = bloom_hash(h, x, bits_mask);
       atomicOr(&w[b & words_mask], 1u << (b >> lw));
     }
@@ -72,8 +79,13 @@ struct Bloom {
   __device__ __forceinline__ bool test(uint32_t x) const {
     bool ok = true;
 #pragma unroll
-    for (int h = 0; h < 10; ++h) {
+    for (int h = 0; h < kUnrolled; ++h) {
       if (h >= nh) break;
+      uint32_t b = bloom_hash(h, x, bits_mask);
+      ok &= ((w[b & words_mask] >> (b >> lw)) & 1u) != 0;
+    }
+#pragma unroll 1
+    for (int h = kUnrolled; h < nh; ++h) {
       uint32_t b = bloom_hash(h, x, bits_mask);
       ok &= ((w[b & words_mask] >> (b >> lw)) & 1u) != 0;
     }
