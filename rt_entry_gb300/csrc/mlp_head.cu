@@ -44,7 +44,8 @@ constexpr int kABytes = kAChunks * kChunkBytes;    // 64 KB
 constexpr int kStageBytes = 256 * kBK * 2;         // one (<= 256) x 64 chunk of a weight matrix
 constexpr int kStages = 5;
 constexpr int kAccCols = 256;                      // columns per TMEM accumulator
-constexpr int kEpiWarps = 8;
+constexpr int kEpiWarps = 16;
+constexpr int kEpiParts = kEpiWarps / 4;           // epilogue warps per TMEM lane quarter
 constexpr int kProducerWarp = kEpiWarps, kMmaWarp = kEpiWarps + 1;
 constexpr int kThreads = 32 * (kEpiWarps + 2);
 constexpr int kSmemBytes = kABytes + kStages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
@@ -202,8 +203,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else {
     // epilogue: warp w owns TMEM lanes (rows) 32q .. 32q+31, q = w % 4, and
-    // one half of the job's columns, h = w / 4
-    const int quarter = warp & 3, half = warp >> 2;
+    // the 32-column chunks part, part + kEpiParts, ... of the job's columns,
+    // part = w / 4 (increasing column order within a thread)
+    const int quarter = warp & 3, part = warp >> 2;
     const int row_l = quarter * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
     int t = 0;
@@ -235,14 +237,19 @@ __global__ void __launch_bounds__(kThreads, 1)
     auto hidden = [&](const float* bias) -> bool {
       if (!wait_full()) return false;
       const int a = t & 1;
-      const int cols = H / 2, c_first = half * cols;
-      for (int c0 = 0; c0 < cols; c0 += 32) {
+      const int nch = H / 32;
+      if (part >= nch) {  // no chunk for this warp: the accumulator is not its to read
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        mbar_arrive(tempty0 + 8 * a);
+      }
+      for (int ch = part; ch < nch; ch += kEpiParts) {
+        const int c = ch * 32;
         uint32_t r[32];
-        tmem_ld32(lane_base + (uint32_t)(a * kAccCols + c_first + c0), r);
+        tmem_ld32(lane_base + (uint32_t)(a * kAccCols + c), r);
         float bv[32];
-        load_bias(bias, c_first + c0, H, bv);
+        load_bias(bias, c, H, bv);
         tmem_wait_ld();
-        if (c0 + 32 >= cols) {  // accumulator drained: hand it back to the MMA issuer
+        if (ch + kEpiParts >= nch) {  // accumulator drained: hand it back to the MMA issuer
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           mbar_arrive(tempty0 + 8 * a);
         }
@@ -256,7 +263,6 @@ __global__ void __launch_bounds__(kThreads, 1)
           __nv_bfloat162 p = __floats2bfloat162_rn(x0, x1);
           pk[i] = *reinterpret_cast<uint32_t*>(&p);
         }
-        const int c = c_first + c0;
         uint8_t* rowp = abuf + (c / kBK) * kChunkBytes + row_l * 128;
         const int u0 = (c % kBK) / 8;
 #pragma unroll
@@ -296,17 +302,18 @@ __global__ void __launch_bounds__(kThreads, 1)
     auto last = [&](int nt) -> bool {
       if (!wait_full()) return false;
       const int a = t & 1;
-      constexpr int cols = BN3 / 2;
-      const int n0 = nt * BN3 + half * cols;
-      const bool full_cols = n0 + cols <= g.N;
+      constexpr int nch = BN3 / 32;
+      static_assert(nch % kEpiParts == 0, "every epilogue warp reads the same number of chunks");
+      const bool full_cols = nt * BN3 + BN3 <= g.N;
 #pragma unroll 1
-      for (int c0 = 0; c0 < cols; c0 += 32) {
+      for (int ch = part; ch < nch; ch += kEpiParts) {
+        const int n0 = nt * BN3 + ch * 32;
         uint32_t r[32];
-        tmem_ld32(lane_base + (uint32_t)(a * kAccCols + half * cols + c0), r);
+        tmem_ld32(lane_base + (uint32_t)(a * kAccCols + ch * 32), r);
         float bv[32];
-        load_bias(g.b3, n0 + c0, g.N, bv);
+        load_bias(g.b3, n0, g.N, bv);
         tmem_wait_ld();
-        if (c0 + 32 >= cols) {
+        if (ch + kEpiParts >= nch) {
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           mbar_arrive(tempty0 + 8 * a);
         }
@@ -316,13 +323,13 @@ __global__ void __launch_bounds__(kThreads, 1)
             const float x = __uint_as_float(r[i]) + bv[i];
             if (x > best[i & 3]) {
               best[i & 3] = x;
-              best_col[i & 3] = n0 + c0 + i;
+              best_col[i & 3] = n0 + i;
             }
           }
         } else {
 #pragma unroll
           for (int i = 0; i < 32; ++i) {
-            const int col = n0 + c0 + i;
+            const int col = n0 + i;
             const float x = col < g.N ? __uint_as_float(r[i]) + bv[i] : -3.402823466e38f;
             if (x > best[i & 3]) {
               best[i & 3] = x;
