@@ -7,13 +7,13 @@
 // the two hidden layers on that block, keeping h1 and then h2 in a 64 KB
 // shared-memory A region in the 128-byte-swizzled K-major layout that the
 // MMA reads, then sweeps its last-layer tiles over the resident h2:
-//   * warp 8 / lane 0 (producer) loads the block's X rows into the A region
+//   * warp 16 / lane 0 (producer) loads the block's X rows into the A region
 //     with TMA once the previous block's MMAs are done with it (`afree`), and
 //     streams 64-wide K chunks of W1, W2 and W3 through a 5-stage ring;
-//   * warp 9 / lane 0 issues tcgen05.mma (M = 128, K = 16, BF16 inputs, FP32
+//   * warp 17 / lane 0 issues tcgen05.mma (M = 128, K = 16, BF16 inputs, FP32
 //     accumulation) into one of two 256-column TMEM accumulators, so that an
 //     epilogue overlaps the next job's MMAs;
-//   * warps 0-7 drain the accumulators: for a hidden layer they add the bias,
+//   * warps 0-15 drain the accumulators: for a hidden layer they add the bias,
 //     apply relu, round to BF16 and write the result into the A region (the
 //     next layer's A operand), then signal `hready`; for the last layer they
 //     keep a running argmax per row and combine it across CTAs with atomicMax
