@@ -48,6 +48,19 @@ def test_null_and_bad_arguments_return_status(lib):
     assert rc == r.RTE_EINVAL
     assert lib.rte_index_load(b"/nonexistent/base.fvecs", b"/nonexistent/g", 0, ctypes.byref(h)) == r.RTE_EIO
     assert lib.rte_search(None, None, 0, None, None, None, None) == r.RTE_EINVAL
+    # the learned head's entry point: NULL arguments, an unknown path and host
+    # pointers (it takes device arrays) are rejected before any GPU work
+    x = np.zeros((4, 8), np.uint16)
+    b = np.zeros(64, np.float32)
+    cols = np.zeros(4, np.int32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    assert lib.rte_mlp_head_argmax(None, 4, 8, None, None, None, None, None, None, 64, 8, 0, None,
+                                   None) == r.RTE_EINVAL
+    assert lib.rte_mlp_head_argmax(P(x), 4, 8, P(x), P(b), P(x), P(b), P(x), P(b), 64, 8, 2, P(cols),
+                                   None) == r.RTE_EINVAL
+    assert lib.rte_mlp_head_argmax(P(x), 4, 8, P(x), P(b), P(x), P(b), P(x), P(b), 64, 8, 0, P(cols),
+                                   None) == r.RTE_EINVAL
+    assert b"device pointers" in lib.rte_last_error()
 
 
 def test_truncated_files_are_rejected(lib, tmp_path):
