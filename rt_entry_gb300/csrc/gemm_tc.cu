@@ -23,6 +23,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "gemm_tc.h"
@@ -446,23 +447,27 @@ cudaError_t gemm_bf16_tn(const GemmArgs& g, cudaStream_t st) {
     return cudaErrorNotSupported;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
-  static int num_sms[64] = {0};
-  static bool attr[2][64] = {{false}};
+  // per-device caches, set once; concurrent host threads may race to set
+  // them, which is harmless (the same values), hence atomics
+  static std::atomic<int> num_sms[64];
+  static std::atomic<bool> attr[2][64];
   if (dev >= 64) return cudaErrorInvalidDevice;
-  if (!attr[wide][dev]) {
+  if (!attr[wide][dev].load(std::memory_order_acquire)) {
     cudaError_t e = wide ? cudaFuncSetAttribute(gemm_bf16_tn_kernel<256>,
                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES)
                          : cudaFuncSetAttribute(gemm_bf16_tn_kernel<128>,
                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    attr[wide][dev] = true;
+    attr[wide][dev].store(true, std::memory_order_release);
   }
   // one CTA per SM, each taking a contiguous range of the output tiles
-  if (num_sms[dev] == 0 &&
-      cudaDeviceGetAttribute(&num_sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    num_sms[dev] = 1;
+  int sms = num_sms[dev].load(std::memory_order_relaxed);
+  if (sms == 0) {
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+    num_sms[dev].store(sms, std::memory_order_relaxed);
+  }
   const long long tiles = (long long)((g.M + BM - 1) / BM) * ((g.N + bn - 1) / bn);
-  dim3 grid((unsigned)(tiles < num_sms[dev] ? tiles : num_sms[dev]));
+  dim3 grid((unsigned)(tiles < sms ? tiles : sms));
   if (wide)
     gemm_bf16_tn_kernel<256><<<grid, kThreads, SMEM_BYTES, st>>>(ma, mb, g);
   else

@@ -27,6 +27,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "gemm_tc.h"
 #include "mlp_head.h"
 #include "tc_common.cuh"
@@ -368,25 +370,29 @@ bool mlp_head_supported(const MlpHeadArgs& a) {
 }
 
 namespace {
-int g_num_sms[64] = {0};
-bool g_attr[2][64] = {{false}};
+// per-device caches, set once; concurrent host threads may race to set them,
+// which is harmless (the same values), hence atomics
+std::atomic<int> g_num_sms[64];
+std::atomic<bool> g_attr[2][64];
 }  // namespace
 
 cudaError_t mlp_head_prepare(int N) {
   const bool wide = N >= 256;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  if (!g_attr[wide][dev]) {
+  if (!g_attr[wide][dev].load(std::memory_order_acquire)) {
     cudaError_t e = wide ? cudaFuncSetAttribute(mlp_head_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 kSmemBytes)
                          : cudaFuncSetAttribute(mlp_head_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 kSmemBytes);
     if (e != cudaSuccess) return e;
-    g_attr[wide][dev] = true;
+    g_attr[wide][dev].store(true, std::memory_order_release);
   }
-  if (g_num_sms[dev] == 0 &&
-      cudaDeviceGetAttribute(&g_num_sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    g_num_sms[dev] = 1;
+  if (g_num_sms[dev].load(std::memory_order_relaxed) == 0) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+    g_num_sms[dev].store(sms, std::memory_order_relaxed);
+  }
   return cudaSuccess;
 }
 
@@ -402,9 +408,9 @@ cudaError_t mlp_head_argmax(const MlpHeadArgs& a, cudaStream_t st) {
   if (pe != cudaSuccess) return pe;
   int dev = 0;
   cudaGetDevice(&dev);
-  int* num_sms = g_num_sms;
+  const int sms = g_num_sms[dev].load(std::memory_order_relaxed);
   const long long tiles = (long long)((a.M + kBM - 1) / kBM) * ((a.N + bn3 - 1) / bn3);
-  const dim3 grid((unsigned)(tiles < num_sms[dev] ? tiles : num_sms[dev]));
+  const dim3 grid((unsigned)(tiles < sms ? tiles : sms));
   if (wide)
     mlp_head_kernel<256><<<grid, kThreads, kSmemBytes, st>>>(mx, m1, m2, m3, a);
   else
