@@ -77,9 +77,15 @@ def build_reference() -> bool:
     return True
 
 
+N_COUNTERS = 6  # fields of Counters
+
+
 class Counters(ctypes.Structure):
+    """Per-query work counters (orc_counters): entries_valid, expanded,
+    dist_evals, iterations, merges, merges_idle."""
     _fields_ = [("entries_valid", ctypes.c_int64), ("expanded", ctypes.c_int64),
-                ("dist_evals", ctypes.c_int64), ("iterations", ctypes.c_int64)]
+                ("dist_evals", ctypes.c_int64), ("iterations", ctypes.c_int64),
+                ("merges", ctypes.c_int64), ("merges_idle", ctypes.c_int64)]
 
 
 def lib():
@@ -155,7 +161,7 @@ def search_multi(base, queries, graph, *, L, k, hits_multi, leaf_pids, search_wi
     if rc != 0:
         raise ValueError("orc_search_multi rejected its arguments")
     if with_counters:
-        return ids, dists, np.frombuffer(cnt, dtype=np.int64).reshape(-1, 4)[:nq].copy()
+        return ids, dists, np.frombuffer(cnt, dtype=np.int64).reshape(-1, N_COUNTERS)[:nq].copy()
     return ids, dists
 
 
@@ -204,7 +210,7 @@ def search(base, queries, graph, *, L, k, search_width=1, max_iter=100, bloom_wo
     if rc != 0:
         raise ValueError("orc_search rejected its arguments")
     if with_counters:
-        c = np.frombuffer(cnt, dtype=np.int64).reshape(-1, 4)[:nq].copy()
+        c = np.frombuffer(cnt, dtype=np.int64).reshape(-1, N_COUNTERS)[:nq].copy()
         return ids, dists, c
     return ids, dists
 
@@ -298,3 +304,75 @@ def ref_pca(x, workdir):
     vec = np.frombuffer(raw, np.float64, d * d, o).reshape(d, d); o += 8 * d * d
     proj = np.frombuffer(raw, np.float32, n * d, o).reshape(n, d)
     return mean.copy(), val.copy(), vec.copy(), proj.copy()
+
+
+# ---- the reference's own search kernel on a GPU (oracle/ref_launch.cpp) ----
+
+def entries_table(leaf_pids, L, np_):
+    """aabb_entries [n_leaves x L] (entry.cu:60-69): entry j of a leaf is its
+    j-th point for j < leaf size, else np."""
+    leaf_pids = np.asarray(leaf_pids)
+    nl, cap = leaf_pids.shape
+    t = np.full((nl, L), np_, np.int32)
+    m = min(cap, L)
+    t[:, :m] = leaf_pids[:, :m]
+    return t
+
+
+def ref_kernel_available(dim):
+    """True when the reference kernel was compiled for this dimension."""
+    return os.path.exists(os.path.join(REF_OUT, f"graph_search_d{dim}.cubin"))
+
+
+class RefKernel:
+    """The reference's GraphSearchKernel, compiled from its own source for
+    sm_103a (oracle/_ref/graph_search_d<dim>.cubin), launched as
+    graph.cu:318-324 launches it.  Uploads base [np x dim] and graph once."""
+
+    def __init__(self, base, graph):
+        base = _c(base, np.float32)
+        graph = _c(graph, np.int32)
+        self.np, self.dim = base.shape
+        cubin = os.path.join(REF_OUT, f"graph_search_d{self.dim}.cubin")
+        if not os.path.exists(cubin):
+            raise FileNotFoundError(f"{cubin} is not built (oracle/ref/Makefile needs the reference tree)")
+        L = ctypes.CDLL(build_ref_launcher())
+        P, I = ctypes.c_void_p, ctypes.c_int
+        L.ref_last_error.restype = ctypes.c_char_p
+        L.ref_open.argtypes = [ctypes.c_char_p, P, I, I, P, I, ctypes.POINTER(P)]
+        L.ref_open.restype = I
+        L.ref_search.argtypes = [P, P, I, P, I, I, P, I, I, I, I, I, I, P, P]
+        L.ref_search.restype = I
+        L.ref_close.argtypes = [P]
+        L.ref_close.restype = None
+        self._lib = L
+        self._h = P()
+        rc = L.ref_open(cubin.encode(), _p(base), self.np, self.dim, _p(graph), graph.shape[1],
+                        ctypes.byref(self._h))
+        if rc != 0:
+            raise RuntimeError(f"ref_open: {L.ref_last_error().decode()}")
+
+    def search(self, queries, entries, hits, L, topk, max_iter=100, algo=1, scrub=False, reps=0):
+        """-> (ids [nq, topk], per-launch device ms [reps])."""
+        q = _c(queries, np.float32)
+        e = _c(entries, np.int32)
+        h = _c(hits, np.int32)
+        nq = q.shape[0]
+        out = np.empty((nq, topk), np.int32)
+        ms = np.zeros(max(reps, 1), np.float32)
+        rc = self._lib.ref_search(self._h, _p(q), nq, _p(e), e.shape[0], L, _p(h), topk, 1, max_iter,
+                                  algo, int(scrub), reps, _p(ms), _p(out))
+        if rc != 0:
+            raise RuntimeError(f"ref_search: {self._lib.ref_last_error().decode()}")
+        return out, ms[:reps].tolist()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ref_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -32,6 +32,10 @@ typedef struct {
   int64_t expanded;        /* X_q: selected nodes whose row was read        */
   int64_t dist_evals;      /* D_q: main-loop distance evaluations           */
   int64_t iterations;      /* main-loop iterations executed                 */
+  int64_t merges;          /* batches merged into the pool (entry + main)   */
+  int64_t merges_idle;     /* of those, batches with no distance below the
+                              pool's largest: the merge leaves the pool as
+                              it was                                        */
 } orc_counters;
 
 /* Beam search over a fixed-degree graph, GraphSearchKernel semantics

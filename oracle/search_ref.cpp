@@ -177,9 +177,18 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
   std::vector<Pair> na(L + B, Pair{ORC_MAX_DIST, np});  // :473-477
   Pair* batch = na.data() + L;
   Bloom bloom(A.bloom_words, A.bloom_hashes);
-  orc_counters c = {0, 0, 0, 0};
+  orc_counters c = {0, 0, 0, 0, 0, 0};
 
   auto dist_of = [&](int id) { return orc_l2_ref(A.base + (int64_t)id * A.d, q, A.d); };
+  // counts a merge, and whether any batch distance is below the pool's
+  // largest (otherwise the merge cannot change the pool)
+  auto count_merge = [&]() {
+    c.merges++;
+    const float pmax = na[L - 1].d;
+    for (int i = 0; i < B; ++i)
+      if (batch[i].d < pmax) return;
+    c.merges_idle++;
+  };
 
   // ---- entry phase (:479-959) ----
   uint32_t seed[64];
@@ -231,6 +240,7 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
         batch[i].d = dist_of(batch[i].id);
         c.entries_valid++;
       }
+    count_merge();
     batch_sort_desc(batch, B);
     merge_pool(na.data(), L, B, false);
   }
@@ -309,6 +319,7 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
       batch[i].d = dist_of(batch[i].id);
       c.dist_evals++;
     }
+    count_merge();
     batch_sort_desc(batch, B);
     merge_pool(na.data(), L, B, true);
     for (iteration = 0; iteration < nchunks; iteration++) {  // :1495-1516

@@ -224,6 +224,24 @@ __device__ __forceinline__ void merge_pool(float (&pd)[pool_regs(NL)], int (&pi)
   }
 }
 
+// True when some batch distance lies strictly below the pool's largest
+// distance (slot L-1: lane 31 of the last register, or lane 15 of the
+// 16-slot pool).  When none does, the merge takes nothing -- it swaps only
+// where pool > batch, and every pool slot is <= the largest -- and the
+// half-cleaner then meets a pool that is still sorted ascending (the pool
+// leaves every merge sorted, and visiting a slot only negates its id), where
+// its strict comparisons swap nothing.  Sorting and merging such a batch
+// therefore leaves the pool unchanged, ids and order included, and
+// search_query skips both.
+template <int NL, int NB>
+__device__ __forceinline__ bool batch_can_enter(const float (&pd)[pool_regs(NL)], const float (&bd)[NB]) {
+  const float pmax = __shfl_sync(kFull, pd[pool_regs(NL) - 1], NL == 0 ? 15 : 31);
+  bool below = false;
+#pragma unroll
+  for (int j = 0; j < NB; ++j) below |= bd[j] < pmax;
+  return __any_sync(kFull, below);
+}
+
 // Partial sum of one lane for one row: s = t0*t0, then fmaf(tc, tc, s) over
 // chunks c (t = p - q on dims lane + 32c).  PREC selects the stored format;
 // BF16 and FP8 rows are widened to FP32 before the subtraction.
@@ -570,8 +588,10 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     }
     __syncwarp();
     c_entries += batch_distances<C, NB, PREC>(a, qv, qx, bd, bi, s_ids, s_dist, lane);
-    sort_batch_desc<NB, true, 32 * NB, kMergeFrom>(bd, bi, lane);
-    merge_pool<NL, NB>(pd, pi, bd, bi, false, lane);
+    if (batch_can_enter<NL, NB>(pd, bd)) {
+      sort_batch_desc<NB, true, 32 * NB, kMergeFrom>(bd, bi, lane);
+      merge_pool<NL, NB>(pd, pi, bd, bi, false, lane);
+    }
   }
 
   // ---- main loop (graph_search.cuh:961-1532) ----
@@ -664,8 +684,10 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     }
 
     c_dists += batch_distances<C, NB, PREC>(a, qv, qx, bd, bi, s_ids, s_dist, lane);
-    sort_batch_desc<NB, true, 32 * NB, kMergeFrom>(bd, bi, lane);
-    merge_pool<NL, NB>(pd, pi, bd, bi, true, lane);
+    if (batch_can_enter<NL, NB>(pd, bd)) {
+      sort_batch_desc<NB, true, 32 * NB, kMergeFrom>(bd, bi, lane);
+      merge_pool<NL, NB>(pd, pi, bd, bi, true, lane);
+    }
 
     bool any = false;
 #pragma unroll 1

@@ -99,7 +99,7 @@ def test_search_matches_oracle_sweep(lib, orc, cuda, d, integer, R, L, W, bw, nh
     assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
     assert np.array_equal(dd, od)
     cnt = idx.counters(q, **kw)
-    assert np.array_equal(cnt, ocnt)
+    assert np.array_equal(cnt, ocnt[:, :4])
     # run twice: bytes identical
     ids2, dd2 = idx.search_projected(q, **kw)
     assert np.array_equal(ids, ids2) and np.array_equal(dd, dd2)

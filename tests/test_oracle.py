@@ -78,6 +78,10 @@ def test_oracle_pool_is_sorted_and_valid(orc):
             if ids[qi, j] < n:
                 assert d[qi, j] == orc.l2_ref(c["base"][ids[qi, j]], c["queries"][qi])
     assert (cnt[:, 0] > 0).all() and (cnt[:, 3] <= 100).all()
+    # merges: one per entry batch and per main-loop iteration that selected
+    # a node; the idle ones (no batch distance below the pool's largest) are
+    # a subset
+    assert (cnt[:, 4] >= 1).all() and (cnt[:, 5] <= cnt[:, 4]).all() and (cnt[:, 5] > 0).any()
 
 
 def test_oracle_l2_matches_fp64_closely(orc):
