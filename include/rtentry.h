@@ -154,12 +154,15 @@ rte_status rte_search_projected(rte_index* idx, const float* projected, const in
  *   - every pointer must be device memory; entry_mode random or kd-tree;
  *   - at most RTE_NOALLOC_MAX_QUERIES queries per call (RTE_EINVAL beyond);
  *   - its scratch (each query's leaf and the search's work counter, about
- *     256 KB) is one fixed array inside the library that every GPU loading
- *     the library holds until the process exits.  The first call on a
- *     device looks up that array's device address, so make the first call
- *     before any stream capture.  All calls share the one array: calls that
- *     overlap on the GPU (other streams, other threads) race on it, so the
- *     caller must not let them overlap. */
+ *     256 KB) is one fixed array inside the library that every GPU holds
+ *     until the process exits.  Creating an index on a device
+ *     (rte_index_from_host, rte_index_load, rte_index_load_dir) looks up the
+ *     array's device address there, which is when the GPU reserves it (CUDA
+ *     loads modules lazily), so the searches themselves reserve nothing.
+ *     Should that lookup fail at index creation, the first call retries it:
+ *     make that call before any stream capture.  All calls share the one
+ *     array: calls that overlap on the GPU (other streams, other threads)
+ *     race on it, so the caller must not let them overlap. */
 #define RTE_NOALLOC_MAX_QUERIES 65536
 rte_status rte_search_projected_noalloc(rte_index* idx, const float* projected,
                                         const int32_t* hits, int64_t nq,
@@ -225,6 +228,35 @@ rte_status rte_get_search_base_lowp(const rte_index* idx, int precision, float* 
  * (minX,minY,minZ,maxX,maxY,maxZ), pids [n_leaves x leaf_size] padded np.
  * Any pointer may be NULL. */
 rte_status rte_get_kdtree(const rte_index* idx, float* tight, float* expanded, int32_t* pids);
+
+/* Open an index from a data directory as the reference leaves it (Graph's
+ * data_name, graph.cu:42-45; RT_Entry::BlockUp, entry.cu:8-77):
+ *   base_path   base vectors: .fvecs, .bvecs, .fbin, .hvecs, .hh or .txt
+ *               (file_read.cu:16-117);
+ *   graph_path  raw int32 [np x degree] (file_read.cu:237-255);
+ *   dir/O.fbin + dir/mean.fbin (pca.cpp:60-90), when present: the PCA is
+ *               installed with keep_dims components (0 = all);
+ *   dir/pca_base.fbin (pca.cpp:128-139), when present: its first keep_dims
+ *               columns become the search space as stored (the reference
+ *               searches exactly these values); otherwise the base is
+ *               projected here;
+ *   dir/<leaf_size>_0.aabbs (entry.cu:171-190), when present and
+ *               leaf_size > 0: the kd-tree is rebuilt over the search space
+ *               and must reproduce the file's leaves and point ids exactly
+ *               (RTE_EIO if not: the file belongs to another base); the
+ *               leaves are then expanded by expand_ratio.
+ * leaf_size <= 0 builds no kd-tree.  Missing PCA files leave the raw base
+ * as the search space (keep_dims must then be 0). */
+rte_status rte_index_load_reference(const char* dir, const char* base_path, const char* graph_path,
+                                    int keep_dims, int leaf_size, float expand_ratio, int device,
+                                    rte_index** out);
+
+/* Reads a vector file by its extension (.fvecs, .bvecs, .fbin, .hvecs, .hh,
+ * .txt; file_read.cu:16-117) on the host, no device needed: *n and *d
+ * receive its shape; with out != NULL the n*d values are copied there
+ * (RTE_EINVAL if capacity < n*d).  Call once with out = NULL to size the
+ * buffer. */
+rte_status rte_read_vectors(const char* path, float* out, int64_t capacity, int64_t* n, int* d);
 
 /* Save / load every built artifact to / from a directory (base.fbin,
  * graph.ibin, mean.fbin, O.fbin, pca_base.fbin and the leaf cache
@@ -343,6 +375,16 @@ rte_status rte_locate_multi(rte_index* idx, const float* projected, int64_t nq, 
  * graph from a file (graph.cu:120); no counterpart. */
 rte_status rte_knn_graph(const float* base, int64_t n, int d, int degree, int device, int32_t* graph,
                          void* stream);
+
+/* Limit of the bounded waits in the tensor-core kernels (the learned head,
+ * its GEMMs and the tensor-core projection), in mbarrier try_wait rounds:
+ * a pipeline wait that runs out records an error, raises a flag the
+ * kernel's other roles poll, lets the copies and MMAs in flight finish,
+ * frees its tensor memory and returns, and synchronous calls report
+ * RTE_ETIMEOUT.  rounds <= 0 restores the default (2^24 rounds, a second or
+ * more).  Process-wide, read at each launch; meant for tests of the timeout
+ * path.  (No reference counterpart.) */
+void rte_set_wait_limit(long long rounds);
 
 /* Message of the last failure on this thread ("" if none). */
 const char* rte_last_error(void);

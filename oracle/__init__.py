@@ -22,7 +22,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_TREE = "/root/reference"
+# The reference's source tree: $RTE_REFERENCE_TREE, else a directory named
+# `reference` beside this repository.  It exists only where fixtures are made.
+REFERENCE_TREE = os.environ.get("RTE_REFERENCE_TREE") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
 LIB = os.path.join(BUILD, "liboracle.so")
 REF_LAUNCH_LIB = os.path.join(BUILD, "liboracle_refgpu.so")
 MAX_DIST = np.float32(536870912.0)

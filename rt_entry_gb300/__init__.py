@@ -32,7 +32,8 @@ EXPORTS = (
     "rte_kdtree_build_host", "rte_sym_eig_host", "rte_get_search_base_lowp", "rte_gemm_bf16",
     "rte_default_train_params", "rte_learned_train", "rte_learned_predict", "rte_mlp_grad_check",
     "rte_search_projected_noalloc", "rte_gemm_bf16_bias_argmax", "rte_mlp_head_argmax", "rte_knn_graph", "rte_locate_multi", "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
-    "rte_batcher_free", "rte_autotune",
+    "rte_batcher_free", "rte_autotune", "rte_set_wait_limit", "rte_index_load_reference",
+    "rte_read_vectors",
 )
 
 
@@ -137,6 +138,10 @@ def load_library(path: str = LIB_PATH):
         "rte_batcher_free": ([P], None),
         "rte_autotune": ([P, P, i64, P, i32, i32, ctypes.c_float, SP,
                           ctypes.POINTER(AutotuneReport)], i32),
+        "rte_set_wait_limit": ([ctypes.c_longlong], None),
+        "rte_index_load_reference": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, i32, i32,
+                                      ctypes.c_float, i32, PP], i32),
+        "rte_read_vectors": ([ctypes.c_char_p, P, i64, ctypes.POINTER(i64), ctypes.POINTER(i32)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -229,6 +234,18 @@ def sym_eig_host(a):
                                            w.ctypes.data_as(ctypes.c_void_p),
                                            v.ctypes.data_as(ctypes.c_void_p)))
     return w, v
+
+
+def read_vectors(path: str) -> np.ndarray:
+    """A vector file as the reference reads it (.fvecs, .bvecs, .fbin,
+    .hvecs, .hh, .txt) -> float32 [n, d], on the host."""
+    L = load_library()
+    n, d = ctypes.c_int64(), ctypes.c_int()
+    _check(L.rte_read_vectors(path.encode(), None, 0, ctypes.byref(n), ctypes.byref(d)))
+    out = np.empty((n.value, d.value), np.float32)
+    _check(L.rte_read_vectors(path.encode(), out.ctypes.data_as(ctypes.c_void_p), out.size,
+                              ctypes.byref(n), ctypes.byref(d)))
+    return out
 
 
 def bf16_bits(x):
@@ -337,6 +354,17 @@ class Index:
         h = ctypes.c_void_p()
         _check(load_library().rte_index_load(base_path.encode(), graph_path.encode(), device,
                                              ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def load_reference(cls, data_dir: str, base_path: str, graph_path: str, keep_dims: int = 0,
+                       leaf_size: int = 0, expand_ratio: float = 0.2, device: int = 0) -> "Index":
+        """An index from the reference's data directory (O.fbin, mean.fbin,
+        pca_base.fbin, <leaf_size>_0.aabbs) plus its base and graph files."""
+        h = ctypes.c_void_p()
+        _check(load_library().rte_index_load_reference(data_dir.encode(), base_path.encode(),
+                                                       graph_path.encode(), keep_dims, leaf_size,
+                                                       expand_ratio, device, ctypes.byref(h)))
         return cls(h)
 
     @classmethod

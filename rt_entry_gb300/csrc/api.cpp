@@ -46,6 +46,10 @@ bool is_device_ptr(const void* p) {
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
+rte_status noalloc_prepare(int dev);
+namespace tc {
+void set_wait_limit(long long rounds);  // tc_common.cuh
+}  // namespace tc
 rte_status learned_leaves(const rte_index* x, const float* d_proj, int64_t nq, int32_t* d_leaf,
                           cudaStream_t st, const uint16_t* xb_in = nullptr,
                           unsigned long long* zkeys = nullptr, int* zerr = nullptr);
@@ -54,7 +58,7 @@ rte_status learned_leaves(const rte_index* x, const float* d_proj, int64_t nq, i
 namespace {
 
 size_t index_bytes(const rte_index* x) {
-  return x->raw.bytes() + x->graph.bytes() + x->d_mean.bytes() + x->d_rot.bytes() +
+  return x->raw.bytes() + x->graph.bytes() + x->d_mean.bytes() + x->d_rot.bytes() + x->d_rot_split.bytes() +
          x->il32.bytes() + x->il16.bytes() + x->il8.bytes() + x->scale8.bytes() + x->norm16.bytes() +
          x->d_nodes.bytes() + x->d_wide.bytes() + x->d_pids.bytes();
 }
@@ -116,6 +120,13 @@ rte_status create_index(const float* base, int64_t np, int dim, const int32_t* g
   }
   if (device < 0 || device >= ndev) return fail(RTE_EINVAL, "device index out of range");
   DeviceGuard g(device);
+  // reserve the allocation-free search's scratch on this device now, while
+  // the caller is still setting up (see noalloc.cu); a failure here only
+  // resurfaces in rte_search_projected_noalloc, which retries the lookup
+  if (noalloc_prepare(device) != RTE_OK) {
+    cudaGetLastError();
+    g_err.clear();
+  }
   std::unique_ptr<rte_index> x(new rte_index());
   x->device = device;
   cudaDeviceGetAttribute(&x->num_sms, cudaDevAttrMultiProcessorCount, device);
@@ -167,10 +178,11 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
   pl.k = prm->k == 0 ? pl.L : prm->k;  // graph.cu:54
   if (pl.k < 0 || pl.k > pl.L) return fail(RTE_EINVAL, "k must be in [1, beam] (topk <= n_candidates)");
   if (pl.L < 16 || pl.L > 256) return fail(RTE_EINVAL, "beam must round to 16..256");
-  if (x->degree < 32) return fail(RTE_EINVAL, "graph degree must be >= 32 for the warp kernel");
+  if (x->degree < 16) return fail(RTE_EINVAL, "graph degree must be >= 16 for the warp kernel");
   if (prm->search_width <= 0) return fail(RTE_EINVAL, "search_width must be >= 1");
   const int B = prm->search_width * x->degree;
-  if (B > 256 || (B & (B - 1))) return fail(RTE_EINVAL, "search_width * degree must be a power of two <= 256");
+  if (B > 256 || (B & (B - 1)))
+    return fail(RTE_EINVAL, "search_width * degree must be a power of two <= 256");
   if (prm->max_iter < 0) return fail(RTE_EINVAL, "max_iter must be >= 0");
   if (prm->bloom_words < 32 || prm->bloom_words > 16384 || (prm->bloom_words & (prm->bloom_words - 1)))
     return fail(RTE_EINVAL, "bloom_words must be a power of two in [32, 16384]");
@@ -189,11 +201,14 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
   if (!search_chunks_supported(x->C))
     return fail(RTE_EINVAL, "search dimension " + std::to_string(x->search_dim) + " has no kernel instantiation");
   pl.NL = pl.L / 32;  // 0 selects the 16-slot pool
-  pl.NB = B / 32;
+  pl.NB = B / 32;     // 0 selects the 16-slot batch (width 1, degree 16)
   pl.prec = prm->precision;
-  // per warp: the bloom filter plus the compaction buffers (ids, distances)
+  // per warp: the bloom filter, the compaction buffers (ids, distances) and
+  // the query slot, whose size depends on the kernel that serves this shape
   const int S = std::max(B, pl.L);
-  const size_t per_warp = (size_t)(prm->bloom_words + 2 * S + kQuerySlotWords) * 4;
+  const bool r16 = x->degree == 16;
+  const int kc = search_kernel_chunks(x->C, pl.NL, pl.NB, pl.prec, r16);
+  const size_t per_warp = (size_t)(prm->bloom_words + 2 * S + query_slot_words_for(kc, x->C)) * 4;
   const size_t smem_cap = 227 * 1024;
   if (prm->warps_per_block > 0) {
     pl.wpb = prm->warps_per_block;
@@ -204,7 +219,7 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
   pl.smem = (size_t)pl.wpb * per_warp;
   if (pl.wpb < 1 || pl.smem > smem_cap)
     return fail(RTE_EINVAL, "bloom filter too large for the block's shared memory");
-  const int occ = occupancy_search(x->C, pl.NL, pl.NB, pl.prec, pl.wpb, pl.smem);
+  const int occ = occupancy_search(x->C, pl.NL, pl.NB, pl.prec, r16, pl.wpb, pl.smem);
   if (occ <= 0)
     return fail(RTE_EINVAL, "no kernel instantiation for beam " + std::to_string(pl.L) + ", batch " +
                                 std::to_string(B) + ", precision " + std::to_string(pl.prec));
@@ -291,11 +306,12 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
       RTE_CUDA(xb.alloc((size_t)nq * x->mlp.dp * 2, st));
       RTE_CUDA(launch_project_bf16(d_queries, nq, x->dim, x->dim, x->d_mean.p, x->d_rot.p,
                                    x->search_dim, x->search_dim, proj.as<float>(), x->search_dim,
-                                   xb.p, x->mlp.in_scale, x->mlp.dp, st, zs.as<uint32_t>(), zwords));
+                                   xb.p, x->mlp.in_scale, x->mlp.dp, st, zs.as<uint32_t>(), zwords,
+                                   x->d_rot_split.p));
     } else {
       RTE_CUDA(launch_project(d_queries, nq, x->dim, x->dim, x->d_mean.p, x->d_rot.p,
                               x->search_dim, x->search_dim, proj.as<float>(), x->search_dim, st,
-                              zs.as<uint32_t>(), zwords));
+                              zs.as<uint32_t>(), zwords, x->d_rot_split.p));
     }
     qp = proj.as<float>();
   }
@@ -433,6 +449,8 @@ void rte_default_params(rte_search_params* p) {
 
 const char* rte_last_error(void) { return g_err.c_str(); }
 
+void rte_set_wait_limit(long long rounds) { rte::tc::set_wait_limit(rounds); }
+
 rte_status rte_index_from_host(const float* base, int64_t np, int dim, const int32_t* graph,
                                int degree, int device, rte_index** out) {
   g_err.clear();
@@ -460,9 +478,14 @@ void rte_index_free(rte_index* idx) {
   delete idx;
 }
 
-rte_status rte_set_pca(rte_index* x, const float* mean, const float* rotation, int keep_dims) {
-  g_err.clear();
-  if (!x || !mean || !rotation) return fail(RTE_EINVAL, "NULL argument");
+}  // extern "C"
+
+namespace {
+// Installs a PCA (mean [dim], rotation [dim x dim]) and makes the first
+// keep_dims components the search space: projected here, or taken from
+// `projected` (host, [np][ld], ld >= keep_dims) when the caller has it.
+rte_status install_pca(rte_index* x, const float* mean, const float* rotation, int keep_dims,
+                       const float* projected, int ld) {
   if (keep_dims == 0) keep_dims = x->dim;
   if (keep_dims < 3 || keep_dims > x->dim) return fail(RTE_EINVAL, "keep_dims must be in [3, dim]");
   DeviceGuard g(x->device);
@@ -482,12 +505,112 @@ rte_status rte_set_pca(rte_index* x, const float* mean, const float* rotation, i
   RTE_CUDA(cudaMemcpy(x->d_mean.p, x->mean32.data(), d * 4, cudaMemcpyHostToDevice));
   RTE_CUDA(x->d_rot.alloc(rk.size()));
   RTE_CUDA(cudaMemcpy(x->d_rot.p, rk.data(), rk.size() * 4, cudaMemcpyHostToDevice));
+  RTE_CUDA(x->d_rot_split.alloc(rotation_split_floats(d, keep_dims)));
+  RTE_CUDA(launch_split_rotation(x->d_rot.p, d, keep_dims, keep_dims, x->d_rot_split.p, 0));
   DevBuf<float> proj;
   RTE_CUDA(proj.alloc((size_t)x->np * keep_dims));
-  RTE_CUDA(launch_project(x->raw.p, x->np, d, d, x->d_mean.p, x->d_rot.p, keep_dims, keep_dims,
-                          proj.p, keep_dims, 0));
+  if (projected) {
+    RTE_CUDA(cudaMemcpy2D(proj.p, (size_t)keep_dims * 4, projected, (size_t)ld * 4, (size_t)keep_dims * 4,
+                          (size_t)x->np, cudaMemcpyHostToDevice));
+  } else {
+    RTE_CUDA(launch_project(x->raw.p, x->np, d, d, x->d_mean.p, x->d_rot.p, keep_dims, keep_dims,
+                            proj.p, keep_dims, 0, nullptr, 0, x->d_rot_split.p));
+  }
   x->has_pca = true;
   return make_search_space(x, proj.p);
+}
+}  // namespace
+
+extern "C" {
+
+rte_status rte_set_pca(rte_index* x, const float* mean, const float* rotation, int keep_dims) {
+  g_err.clear();
+  if (!x || !mean || !rotation) return fail(RTE_EINVAL, "NULL argument");
+  return install_pca(x, mean, rotation, keep_dims, nullptr, 0);
+}
+
+rte_status rte_index_load_reference(const char* dir, const char* base_path, const char* graph_path,
+                                    int keep_dims, int leaf_size, float expand_ratio, int device,
+                                    rte_index** out) {
+  g_err.clear();
+  if (!dir || !base_path || !graph_path || !out) return fail(RTE_EINVAL, "NULL argument");
+  *out = nullptr;
+  std::string err;
+  std::vector<float> base;
+  int64_t np = 0;
+  int dim = 0;
+  if (!io::read_vectors(base_path, base, np, dim, err)) return fail(RTE_EIO, err);
+  std::vector<int32_t> graph;
+  int degree = 0;
+  if (!io::read_graph(graph_path, np, graph, degree, err)) return fail(RTE_EIO, err);
+  rte_index* raw = nullptr;
+  rte_status s = create_index(base.data(), np, dim, graph.data(), degree, device, &raw);
+  if (s != RTE_OK) return s;
+  std::unique_ptr<rte_index, void (*)(rte_index*)> x(raw, rte_index_free);
+  base.clear();
+  base.shrink_to_fit();
+  const std::string D(dir);
+  const bool has_o = io::file_exists(D + "/O.fbin"), has_m = io::file_exists(D + "/mean.fbin");
+  if (has_o != has_m) return fail(RTE_EIO, D + ": O.fbin and mean.fbin must both be present or both absent");
+  if (has_o) {
+    std::vector<float> mean, rot;
+    int64_t n1 = 0;
+    int d1 = 0;
+    if (!io::read_matrix_fbin(D + "/mean.fbin", mean, n1, d1, err)) return fail(RTE_EIO, err);
+    if (n1 != 1 || d1 != dim) return fail(RTE_EIO, D + "/mean.fbin is not [1 x " + std::to_string(dim) + "]");
+    if (!io::read_matrix_fbin(D + "/O.fbin", rot, n1, d1, err)) return fail(RTE_EIO, err);
+    if (n1 != dim || d1 != dim)
+      return fail(RTE_EIO, D + "/O.fbin is not [" + std::to_string(dim) + " x " + std::to_string(dim) + "]");
+    const int keep = keep_dims == 0 ? dim : keep_dims;
+    if (keep < 3 || keep > dim) return fail(RTE_EINVAL, "keep_dims must be in [3, dim]");
+    std::vector<float> pb;
+    int pd = 0;
+    if (io::file_exists(D + "/pca_base.fbin")) {
+      int64_t pn = 0;
+      if (!io::read_matrix_fbin(D + "/pca_base.fbin", pb, pn, pd, err)) return fail(RTE_EIO, err);
+      if (pn != np || pd < keep)
+        return fail(RTE_EIO, D + "/pca_base.fbin is [" + std::to_string(pn) + " x " + std::to_string(pd) +
+                                 "], the base needs [" + std::to_string(np) + " x >= " + std::to_string(keep) + "]");
+    }
+    s = install_pca(x.get(), mean.data(), rot.data(), keep, pb.empty() ? nullptr : pb.data(), pd);
+    if (s != RTE_OK) return s;
+  } else if (keep_dims != 0) {
+    return fail(RTE_EIO, D + ": keep_dims given but no O.fbin / mean.fbin");
+  }
+  if (leaf_size > 0) {
+    s = rte_build_kdtree(x.get(), leaf_size, expand_ratio);
+    if (s != RTE_OK) return s;
+    const std::string af = D + "/" + std::to_string(leaf_size) + "_0.aabbs";
+    if (io::file_exists(af)) {
+      int64_t nl = 0;
+      int ls = 0;
+      std::vector<float> boxes;
+      std::vector<int32_t> pids;
+      if (!io::read_aabbs(af, nl, ls, boxes, pids, err)) return fail(RTE_EIO, err);
+      if (nl != x->kd.n_leaves || ls != x->kd.cap || boxes != x->kd.tight || pids != x->kd.pids)
+        return fail(RTE_EIO, af + " does not hold the kd-tree of this search space (" + std::to_string(nl) +
+                                 " leaves in the file, " + std::to_string(x->kd.n_leaves) + " built)");
+    }
+  }
+  *out = x.release();
+  return RTE_OK;
+}
+
+rte_status rte_read_vectors(const char* path, float* out, int64_t capacity, int64_t* n, int* d) {
+  g_err.clear();
+  if (!path || !n || !d) return fail(RTE_EINVAL, "NULL argument");
+  std::vector<float> data;
+  int64_t n0 = 0;
+  int d0 = 0;
+  std::string err;
+  if (!io::read_vectors(path, data, n0, d0, err)) return fail(RTE_EIO, err);
+  *n = n0;
+  *d = d0;
+  if (!out) return RTE_OK;
+  if (capacity < (int64_t)data.size())
+    return fail(RTE_EINVAL, "capacity " + std::to_string(capacity) + " < n*d = " + std::to_string(data.size()));
+  std::copy(data.begin(), data.end(), out);
+  return RTE_OK;
 }
 
 rte_status rte_build_pca(rte_index* x, int keep_dims) {
@@ -567,7 +690,7 @@ rte_status rte_project(rte_index* x, const float* queries, int64_t nq, float* ou
   }
   if (x->has_pca) {
     RTE_CUDA(launch_project(dq, nq, x->dim, x->dim, x->d_mean.p, x->d_rot.p, x->search_dim,
-                            x->search_dim, dout, x->search_dim, st));
+                            x->search_dim, dout, x->search_dim, st, nullptr, 0, x->d_rot_split.p));
   } else {
     RTE_CUDA(cudaMemcpyAsync(dout, dq, (size_t)nq * x->dim * 4, cudaMemcpyDeviceToDevice, st));
   }

@@ -85,7 +85,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tempty0 = smem_u32(bars + 2 * kMaxStages + 2);  // accumulator a drained
   const uint32_t afull = smem_u32(bars + 2 * kMaxStages + 4);  // resident A block landed
   const uint32_t afree = smem_u32(bars + 2 * kMaxStages + 5);  // MMAs done with the A block
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kMaxStages + 6);
+  const uint32_t drain = smem_u32(bars + 2 * kMaxStages + 6);  // every MMA issued has completed
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kMaxStages + 7);
   __shared__ int s_abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -116,6 +117,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     mbar_init(afull, 1);
     mbar_init(afree, 1);
+    mbar_init(drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == kMmaWarp) {
@@ -138,7 +140,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int mt = (int)(ti / n_tiles), nt = (int)(ti % n_tiles);
         if (resident && mt != cur_mt) {
           // a new row block: wait until the MMAs are done with the old one
-          if (a_loads > 0 && !mbar_wait(afree, (a_loads - 1) & 1, g.err, 6, abort)) {
+          if (a_loads > 0 && !mbar_wait(afree, (a_loads - 1) & 1, g.err, 6, abort, g.wait_limit)) {
             ok = false;
             break;
           }
@@ -149,7 +151,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         for (int kt = 0; kt < nk; ++kt) {
           const int s = issued % nst, r = issued / nst;
-          if (issued >= nst && !mbar_wait(empty0 + 8 * s, (r - 1) & 1, g.err, 1, abort)) {
+          if (issued >= nst && !mbar_wait(empty0 + 8 * s, (r - 1) & 1, g.err, 1, abort, g.wait_limit)) {
             ok = false;
             break;
           }
@@ -177,7 +179,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int mt = (int)(ti / n_tiles);
         if (resident && mt != cur_mt) {
           if (cur_mt >= 0) mma_commit(afree);  // arrives once the MMAs on the old block finish
-          if (!mbar_wait(afull, a_uses & 1, g.err, 3, abort)) {
+          if (!mbar_wait(afull, a_uses & 1, g.err, 3, abort, g.wait_limit)) {
             ok = false;
             break;
           }
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           cur_mt = mt;
         }
         const int a = t & 1;
-        if (t >= 2 && !mbar_wait(tempty0 + 8 * a, ((t >> 1) - 1) & 1, g.err, 5, abort)) {
+        if (t >= 2 && !mbar_wait(tempty0 + 8 * a, ((t >> 1) - 1) & 1, g.err, 5, abort, g.wait_limit)) {
           ok = false;
           break;
         }
@@ -193,7 +195,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t d = tmem + (uint32_t)(a * BN);
         for (int kt = 0; kt < nk; ++kt, ++used) {
           const int s = used % nst, r = used / nst;
-          if (!mbar_wait(full0 + 8 * s, r & 1, g.err, 3, abort)) {
+          if (!mbar_wait(full0 + 8 * s, r & 1, g.err, 3, abort, g.wait_limit)) {
             ok = false;
             break;
           }
@@ -209,6 +211,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         mma_commit(tfull0 + 8 * a);
       }
       if (!ok) *(volatile int*)abort = 1;
+      // no MMA may still run when TMEM is freed, whatever path led here
+      mma_commit(drain);
+      mbar_wait(drain, 0, g.err, 7);
     }
   } else {
     // epilogue: warp w owns accumulator rows 32q .. 32q+31 (TMEM lanes,
@@ -256,7 +261,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       cur_mt = mt;
       const int a = t & 1;
-      const bool ok = __all_sync(0xffffffffu, mbar_wait(tfull0 + 8 * a, (t >> 1) & 1, g.err, 4, abort));
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(tfull0 + 8 * a, (t >> 1) & 1, g.err, 4, abort, g.wait_limit));
       if (!ok) {
         *(volatile int*)abort = 1;
         cur_mt = -1;
@@ -415,6 +420,28 @@ static EncodeTiledFn encoder() {
   return fn;
 }
 
+namespace {
+std::atomic<long long> g_wait_limit{kWaitLimit};
+}  // namespace
+
+long long wait_limit() { return g_wait_limit.load(std::memory_order_relaxed); }
+void set_wait_limit(long long rounds) {
+  g_wait_limit.store(rounds > 0 ? rounds : kWaitLimit, std::memory_order_relaxed);
+}
+
+bool make_map_f32(CUtensorMap* m, const void* base, int64_t rows, int cols, int64_t pitch, int box_k,
+                  int box_rows) {
+  EncodeTiledFn enc = encoder();
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)pitch * 4};
+  cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box,
+             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 bool make_map_bf16(CUtensorMap* m, const void* base, int rows, int K, int box_k, int box_rows) {
   EncodeTiledFn enc = encoder();
   if (!enc) return false;
@@ -468,10 +495,12 @@ cudaError_t gemm_bf16_tn(const GemmArgs& g, cudaStream_t st) {
   }
   const long long tiles = (long long)((g.M + BM - 1) / BM) * ((g.N + bn - 1) / bn);
   dim3 grid((unsigned)(tiles < sms ? tiles : sms));
+  GemmArgs ga = g;
+  ga.wait_limit = wait_limit();
   if (wide)
-    gemm_bf16_tn_kernel<256><<<grid, kThreads, SMEM_BYTES, st>>>(ma, mb, g);
+    gemm_bf16_tn_kernel<256><<<grid, kThreads, SMEM_BYTES, st>>>(ma, mb, ga);
   else
-    gemm_bf16_tn_kernel<128><<<grid, kThreads, SMEM_BYTES, st>>>(ma, mb, g);
+    gemm_bf16_tn_kernel<128><<<grid, kThreads, SMEM_BYTES, st>>>(ma, mb, ga);
   return cudaGetLastError();
 }
 

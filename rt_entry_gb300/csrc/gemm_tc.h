@@ -29,6 +29,7 @@ struct GemmArgs {
   const float* bias;    // [N] or null
   unsigned long long* out_argmax;  // [M], packed key (see gemm_tc.cu), pre-set to 0
   int* err;             // device flag: set to a non-zero code when a bounded wait runs out
+  long long wait_limit; // try_wait rounds of the pipeline waits (set by gemm_bf16_tn)
 };
 
 // Returns cudaErrorInvalidValue for unsupported shapes, cudaErrorNotSupported

@@ -128,6 +128,7 @@ struct rte_index {
   std::vector<double> mean64, eig64, vec64;  // vec64[dim][dim], column = component
   std::vector<float> mean32, rot32;          // rot32[dim][dim]
   rte::DevBuf<float> d_mean, d_rot;          // d_rot[dim][search_dim]
+  rte::DevBuf<float> d_rot_split;            // d_rot split for the tensor cores (launch_split_rotation)
   // search space
   int C = 0;
   rte::DevBuf<float> il32;

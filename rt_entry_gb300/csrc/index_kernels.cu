@@ -576,8 +576,13 @@ cudaError_t launch_cov(const float* x, int64_t n, int d, const double* mean, dou
 
 cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const float* mean,
                            const float* V, int vstride, int k, float* out, int ostride,
-                           cudaStream_t st, uint32_t* zero, int64_t zero_words) {
+                           cudaStream_t st, uint32_t* zero, int64_t zero_words, const float* vt_split) {
   if (n == 0) return cudaSuccess;
+  if (vt_split) {
+    const cudaError_t e = launch_project_tc(x, n, nullptr, d, xstride, mean, vt_split, k, out, ostride, nullptr,
+                                            0.0f, 0, zero, zero_words, nullptr, st);
+    if (e != cudaErrorNotSupported) return e;
+  }
   dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
   project_rows<false><<<grid, kPrThreads, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride,
                                             nullptr, nullptr, 0.0f, 0, zero, zero_words);
@@ -587,9 +592,14 @@ cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const 
 cudaError_t launch_project_bf16(const float* x, int64_t n, int d, int xstride, const float* mean,
                                 const float* V, int vstride, int k, float* out, int ostride,
                                 void* out16, float s16, int ld16, cudaStream_t st, uint32_t* zero,
-                                int64_t zero_words) {
+                                int64_t zero_words, const float* vt_split) {
   if (n == 0) return cudaSuccess;
   if (ld16 < k || ld16 > ((k + kPrCols - 1) / kPrCols) * kPrCols) return cudaErrorInvalidValue;
+  if (vt_split) {
+    const cudaError_t e = launch_project_tc(x, n, nullptr, d, xstride, mean, vt_split, k, out, ostride, out16,
+                                            s16, ld16, zero, zero_words, nullptr, st);
+    if (e != cudaErrorNotSupported) return e;
+  }
   dim3 grid((unsigned)((n + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
   project_rows<true><<<grid, kPrThreads, 0, st>>>(x, n, d, xstride, mean, V, vstride, k, out, ostride, nullptr,
                                            reinterpret_cast<__nv_bfloat16*>(out16), s16, ld16, zero,
@@ -599,7 +609,12 @@ cudaError_t launch_project_bf16(const float* x, int64_t n, int d, int xstride, c
 
 cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, int d, int xstride,
                                const float* mean, const float* V, int vstride, int k, float* out,
-                               int ostride, cudaStream_t st) {
+                               int ostride, cudaStream_t st, const float* vt_split) {
+  if (vt_split) {
+    const cudaError_t e = launch_project_tc(x, cap, n_dev, d, xstride, mean, vt_split, k, out, ostride, nullptr,
+                                            0.0f, 0, nullptr, 0, nullptr, st);
+    if (e != cudaErrorNotSupported) return e;
+  }
   dim3 grid((unsigned)((cap + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
   project_rows<false><<<grid, kPrThreads, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride,
                                             n_dev, nullptr, 0.0f, 0, nullptr, 0);
@@ -609,8 +624,13 @@ cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, in
 cudaError_t launch_project_bf16_dyn(const float* x, int64_t cap, const int* n_dev, int d, int xstride,
                                     const float* mean, const float* V, int vstride, int k, float* out,
                                     int ostride, void* out16, float s16, int ld16, uint32_t* zero,
-                                    int64_t zero_words, cudaStream_t st) {
+                                    int64_t zero_words, cudaStream_t st, const float* vt_split) {
   if (ld16 < k || ld16 > ((k + kPrCols - 1) / kPrCols) * kPrCols) return cudaErrorInvalidValue;
+  if (vt_split) {
+    const cudaError_t e = launch_project_tc(x, cap, n_dev, d, xstride, mean, vt_split, k, out, ostride, out16,
+                                            s16, ld16, zero, zero_words, nullptr, st);
+    if (e != cudaErrorNotSupported) return e;
+  }
   dim3 grid((unsigned)((cap + kPrRows - 1) / kPrRows), (k + kPrCols - 1) / kPrCols);
   project_rows<true><<<grid, kPrThreads, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride, n_dev,
                                                   reinterpret_cast<__nv_bfloat16*>(out16), s16, ld16, zero,

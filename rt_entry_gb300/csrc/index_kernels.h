@@ -38,29 +38,48 @@ cudaError_t launch_mean(const float* x, int64_t n, int d, double* partial, int n
                         double* mean, cudaStream_t st);
 cudaError_t launch_cov(const float* x, int64_t n, int d, const double* mean, double* partial,
                        int nchunks, double* cov, cudaStream_t st);
+// The projection out[r][c] = sum_k (x[r][k] - mean[k]) V[k][c], c < k.
+// vt_split: the rotation split for the tensor cores (launch_split_rotation);
+// when it is given and x meets the tensor map's alignment (16-byte base,
+// row pitch a multiple of 4 floats) the product runs on tcgen05
+// (project_tc.cu), otherwise on the FP32 FMA kernel.
 // zero / zero_words: a word range the kernel also sets to 0 (a query call's
 // work counter, error flag and argmax keys), so that the call needs no
 // separate memsets.
 cudaError_t launch_project(const float* x, int64_t n, int d, int xstride, const float* mean,
                            const float* V, int vstride, int k, float* out, int ostride,
-                           cudaStream_t st, uint32_t* zero = nullptr, int64_t zero_words = 0);
+                           cudaStream_t st, uint32_t* zero = nullptr, int64_t zero_words = 0,
+                           const float* vt_split = nullptr);
 // launch_project plus a BF16 copy of the output: out16[r][c] =
 // bf16(out[r][c] * s16) for c < k, 0 for k <= c < ld16 (the learned head's
 // input rows, ld16 >= k).
 cudaError_t launch_project_bf16(const float* x, int64_t n, int d, int xstride, const float* mean,
                                 const float* V, int vstride, int k, float* out, int ostride,
                                 void* out16, float s16, int ld16, cudaStream_t st,
-                                uint32_t* zero = nullptr, int64_t zero_words = 0);
+                                uint32_t* zero = nullptr, int64_t zero_words = 0,
+                                const float* vt_split = nullptr);
 // Variants for graph replay: grids sized for `cap` rows, the live row count
 // read from device memory at run time.
 cudaError_t launch_project_dyn(const float* x, int64_t cap, const int* n_dev, int d, int xstride,
                                const float* mean, const float* V, int vstride, int k, float* out,
-                               int ostride, cudaStream_t st);
+                               int ostride, cudaStream_t st, const float* vt_split = nullptr);
 // launch_project_bf16 for graph replay, plus the zeroed word range.
 cudaError_t launch_project_bf16_dyn(const float* x, int64_t cap, const int* n_dev, int d, int xstride,
                                     const float* mean, const float* V, int vstride, int k, float* out,
                                     int ostride, void* out16, float s16, int ld16, uint32_t* zero,
-                                    int64_t zero_words, cudaStream_t st);
+                                    int64_t zero_words, cudaStream_t st, const float* vt_split = nullptr);
+// The rotation V [d][k] (row pitch vstride) split for the tensor cores:
+// [2][k][round_up(d, 4)] floats, V^T rounded to TF32 then the TF32 of the
+// remainder (project_tc.cu).
+size_t rotation_split_floats(int d, int k);
+cudaError_t launch_split_rotation(const float* V, int d, int k, int vstride, float* out, cudaStream_t st);
+// The tensor-core projection (project_tc.cu); cudaErrorNotSupported when the
+// shapes or alignments do not fit it.  err: set to a non-zero code when a
+// bounded pipeline wait runs out (may be null).
+cudaError_t launch_project_tc(const float* x, int64_t n, const int* n_dev, int d, int xstride,
+                              const float* mean, const float* vt_split, int k, float* out, int ostride,
+                              void* out16, float s16, int ld16, uint32_t* zero, int64_t zero_words,
+                              int* err, cudaStream_t st);
 cudaError_t launch_locate_dyn(const WideNode* wide, int n_wide, const float* pts, int64_t cap,
                               const int* n_dev, int stride, int32_t* out, cudaStream_t st, bool top_cache = true);
 cudaError_t launch_interleave(const float* src, int64_t n, int d, int C, float* il32, void* il16,

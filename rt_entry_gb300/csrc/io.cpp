@@ -119,15 +119,90 @@ bool write_all(const std::string& path, const void* a, size_t na, const void* b,
   return true;
 }
 
+// int32 d, then n*d floats with n = (size - 4) / (4d): the .hvecs and .hh
+// layouts (file_read.cu:83-101 and :171-193, whose readers infer n the
+// same way).
+bool read_dhead(const std::string& path, std::vector<float>& data, int64_t& n, int& d,
+                std::string& err) {
+  int64_t sz;
+  if (!file_size(path, sz, err)) return false;
+  File fh;
+  fh.f = fopen(path.c_str(), "rb");
+  if (!fh.f) {
+    err = "cannot open " + path;
+    return false;
+  }
+  int32_t d0 = 0;
+  if (sz < 4 || fread(&d0, 4, 1, fh.f) != 1 || d0 <= 0) {
+    err = path + ": bad header";
+    return false;
+  }
+  if ((sz - 4) % ((int64_t)d0 * 4) != 0) {
+    err = path + ": size is not 4 + a multiple of 4d (truncated?)";
+    return false;
+  }
+  n = (sz - 4) / ((int64_t)d0 * 4);
+  d = d0;
+  data.resize((size_t)n * d);
+  if (fread(data.data(), 4, data.size(), fh.f) != data.size()) {
+    err = path + ": short read";
+    return false;
+  }
+  return true;
+}
+
+// Text: "n d", then n rows of d values separated by commas (the last value
+// of a row without one), file_read.cu:103-117.  Whitespace between values
+// is accepted too.
+bool read_txt(const std::string& path, std::vector<float>& data, int64_t& n, int& d, std::string& err) {
+  File fh;
+  fh.f = fopen(path.c_str(), "r");
+  if (!fh.f) {
+    err = "cannot open " + path;
+    return false;
+  }
+  long long n0 = 0;
+  int d0 = 0;
+  if (fscanf(fh.f, "%lld %d", &n0, &d0) != 2 || n0 < 0 || d0 <= 0) {
+    err = path + ": bad header (expected \"n d\")";
+    return false;
+  }
+  n = n0;
+  d = d0;
+  data.resize((size_t)n * d);
+  for (size_t i = 0; i < data.size(); ++i) {
+    if (fscanf(fh.f, " %f", &data[i]) != 1) {
+      err = path + ": expected " + std::to_string(data.size()) + " values, read " + std::to_string(i);
+      return false;
+    }
+    int c = fgetc(fh.f);
+    while (c == ' ' || c == '\t' || c == '\r' || c == '\n') c = fgetc(fh.f);
+    if (c != ',' && c != EOF) ungetc(c, fh.f);
+  }
+  return true;
+}
+
 }  // namespace
+
+bool file_exists(const std::string& path) {
+  struct stat st;
+  return stat(path.c_str(), &st) == 0;
+}
 
 bool read_vectors(const std::string& path, std::vector<float>& data, int64_t& n, int& d,
                   std::string& err) {
   if (ends_with(path, ".fvecs")) return read_framed<float>(path, data, n, d, err);
   if (ends_with(path, ".bvecs")) return read_framed<uint8_t>(path, data, n, d, err);
   if (ends_with(path, ".fbin")) return read_fbin(path, data, n, d, err);
-  err = path + ": unknown vector format (expected .fvecs, .bvecs or .fbin)";
+  if (ends_with(path, ".hvecs") || ends_with(path, ".hh")) return read_dhead(path, data, n, d, err);
+  if (ends_with(path, ".txt")) return read_txt(path, data, n, d, err);
+  err = path + ": unknown vector format (expected .fvecs, .bvecs, .fbin, .hvecs, .hh or .txt)";
   return false;
+}
+
+bool read_matrix_fbin(const std::string& path, std::vector<float>& data, int64_t& n, int& d,
+                      std::string& err) {
+  return read_fbin(path, data, n, d, err);
 }
 
 bool read_ivecs(const std::string& path, std::vector<int32_t>& data, int64_t& n, int& d,

@@ -9,6 +9,10 @@
 //   <leaf_size>_0.aabbs        int32 n_leaves, int32 leaf_size, 6 floats per
 //                              tight leaf box, int32 pids [n_leaves x
 //                              leaf_size] (entry.cu:171-190)
+//   .hvecs / .hh               int32 d, then n*d float, n from the file size
+//                              (file_read.cu:83-101, :171-193)
+//   .txt                       "n d", then rows of comma-separated values
+//                              (file_read.cu:103-117)
 #pragma once
 #include <stdint.h>
 
@@ -18,8 +22,13 @@
 namespace rte {
 namespace io {
 
+bool file_exists(const std::string& path);
+// Vectors by extension: .fvecs .bvecs .fbin .hvecs .hh .txt (file_read.cu:16-80).
 bool read_vectors(const std::string& path, std::vector<float>& data, int64_t& n, int& d,
                   std::string& err);
+// An .fbin matrix whatever its name (mean.fbin, O.fbin, pca_base.fbin).
+bool read_matrix_fbin(const std::string& path, std::vector<float>& data, int64_t& n, int& d,
+                      std::string& err);
 bool read_ivecs(const std::string& path, std::vector<int32_t>& data, int64_t& n, int& d,
                 std::string& err);
 bool read_graph(const std::string& path, int64_t np, std::vector<int32_t>& data, int& degree,

@@ -252,8 +252,9 @@ void subtree_classes(const KdTree& t, int depth, std::vector<int32_t>& leaf_clas
 // Buffers of one optimisation step on a batch of M rows.
 struct StepBufs {
   DevBuf<uint16_t> H1, H2, dZ, dZT, H2T, W3T, dH2, dH2T, H1T, W2T, dH1, dH1T, XT;
-  DevBuf<float> Z, dH2f, dH1f, loss;
+  DevBuf<float> Z, dH2f, dH1f, loss, colpart;
   rte_status alloc(int M, int H, int C, int dp) {
+    RTE_CUDA(colpart.alloc((size_t)col_sum_slices(M) * std::max(H, C)));
     RTE_CUDA(H1.alloc((size_t)M * H));
     RTE_CUDA(H2.alloc((size_t)M * H));
     RTE_CUDA(Z.alloc((size_t)M * C));
@@ -289,7 +290,7 @@ rte_status fwd_bwd(const Mlp& m, const uint16_t* Xb, const int32_t* yb, int M, S
   RTE_CUDA(launch_transpose_bf16(b.dZ.p, M, C, b.dZT.p, st));
   RTE_CUDA(launch_transpose_bf16(b.H2.p, M, H, b.H2T.p, st));
   RTE_CUDA(gemm(b.dZT.p, b.H2T.p, C, H, M, kEpiStoreF32, gw[2], H, nullptr, nullptr, err, st));
-  RTE_CUDA(launch_col_sum_bf16(b.dZ.p, M, C, gb[2], st));
+  RTE_CUDA(launch_col_sum_bf16(b.dZ.p, M, C, gb[2], b.colpart.p, st));
   RTE_CUDA(launch_transpose_bf16(m.W16[2].p, C, H, b.W3T.p, st));
   RTE_CUDA(gemm(b.dZ.p, b.W3T.p, M, H, C, kEpiStoreF32, b.dH2f.p, H, nullptr, nullptr, err, st));
   RTE_CUDA(launch_relu_grad(b.dH2f.p, b.H2.p, (int64_t)M * H, b.dH2.p, st));
@@ -297,7 +298,7 @@ rte_status fwd_bwd(const Mlp& m, const uint16_t* Xb, const int32_t* yb, int M, S
   RTE_CUDA(launch_transpose_bf16(b.dH2.p, M, H, b.dH2T.p, st));
   RTE_CUDA(launch_transpose_bf16(b.H1.p, M, H, b.H1T.p, st));
   RTE_CUDA(gemm(b.dH2T.p, b.H1T.p, H, H, M, kEpiStoreF32, gw[1], H, nullptr, nullptr, err, st));
-  RTE_CUDA(launch_col_sum_bf16(b.dH2.p, M, H, gb[1], st));
+  RTE_CUDA(launch_col_sum_bf16(b.dH2.p, M, H, gb[1], b.colpart.p, st));
   RTE_CUDA(launch_transpose_bf16(m.W16[1].p, H, H, b.W2T.p, st));
   RTE_CUDA(gemm(b.dH2.p, b.W2T.p, M, H, H, kEpiStoreF32, b.dH1f.p, H, nullptr, nullptr, err, st));
   RTE_CUDA(launch_relu_grad(b.dH1f.p, b.H1.p, (int64_t)M * H, b.dH1.p, st));
@@ -305,7 +306,7 @@ rte_status fwd_bwd(const Mlp& m, const uint16_t* Xb, const int32_t* yb, int M, S
   RTE_CUDA(launch_transpose_bf16(b.dH1.p, M, H, b.dH1T.p, st));
   RTE_CUDA(launch_transpose_bf16(Xb, M, dp, b.XT.p, st));
   RTE_CUDA(gemm(b.dH1T.p, b.XT.p, H, dp, M, kEpiStoreF32, gw[0], dp, nullptr, nullptr, err, st));
-  RTE_CUDA(launch_col_sum_bf16(b.dH1.p, M, H, gb[0], st));
+  RTE_CUDA(launch_col_sum_bf16(b.dH1.p, M, H, gb[0], b.colpart.p, st));
   return RTE_OK;
 }
 
@@ -440,7 +441,8 @@ extern "C" rte_status rte_learned_train(rte_index* x, const float* train_queries
   RTE_CUDA(cudaMemcpy(q32.p, train_queries, q32.bytes(), cudaMemcpyDefault));
   RTE_CUDA(proj.alloc((size_t)n * d));
   if (x->has_pca) {
-    RTE_CUDA(launch_project(q32.p, n, x->dim, x->dim, x->d_mean.p, x->d_rot.p, d, d, proj.p, d, st));
+    RTE_CUDA(launch_project(q32.p, n, x->dim, x->dim, x->d_mean.p, x->d_rot.p, d, d, proj.p, d, st,
+                            nullptr, 0, x->d_rot_split.p));
   } else {
     RTE_CUDA(cudaMemcpy(proj.p, q32.p, proj.bytes(), cudaMemcpyDeviceToDevice));
   }

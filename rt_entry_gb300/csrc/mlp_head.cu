@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       // one weight chunk into the next ring stage
       auto push = [&](const CUtensorMap* map, int x, int y, uint32_t bytes) -> bool {
         const int s = issued % kStages, r = issued / kStages;
-        if (issued >= kStages && !mbar_wait(empty0 + 8 * s, (r - 1) & 1, g.err, 11, abort)) return false;
+        if (issued >= kStages && !mbar_wait(empty0 + 8 * s, (r - 1) & 1, g.err, 11, abort, g.wait_limit)) return false;
         if (*(volatile int*)abort) return false;
         mbar_expect_tx(full0 + 8 * s, bytes);
         tma_load_2d(smem_u32(ring + s * kStageBytes), map, x, y, full0 + 8 * s);
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint32_t hbytes = (uint32_t)H * kBK * 2, w3bytes = (uint32_t)BN3 * kBK * 2;
       for (int rb = rb_first; rb <= rb_last && ok; ++rb) {
         const int rbi = rb - rb_first;
-        if (rbi > 0 && !mbar_wait(afree, (rbi - 1) & 1, g.err, 12, abort)) {
+        if (rbi > 0 && !mbar_wait(afree, (rbi - 1) & 1, g.err, 12, abort, g.wait_limit)) {
           ok = false;
           break;
         }
@@ -164,12 +164,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       // one job: nk chunks of K into accumulator t & 1
       auto job = [&](int nk, uint32_t idesc) -> bool {
         const int a = t & 1;
-        if (t >= 2 && !mbar_wait(tempty0 + 8 * a, ((t >> 1) - 1) & 1, g.err, 15, abort)) return false;
+        if (t >= 2 && !mbar_wait(tempty0 + 8 * a, ((t >> 1) - 1) & 1, g.err, 15, abort, g.wait_limit)) return false;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t d = tmem + (uint32_t)(a * kAccCols);
         for (int kc = 0; kc < nk; ++kc, ++used) {
           const int s = used % kStages, r = used / kStages;
-          if (!mbar_wait(full0 + 8 * s, r & 1, g.err, 16, abort)) return false;
+          if (!mbar_wait(full0 + 8 * s, r & 1, g.err, 16, abort, g.wait_limit)) return false;
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint64_t ad = sw128_desc(smem_u32(abuf + kc * kChunkBytes));
           const uint64_t bd = sw128_desc(smem_u32(ring + s * kStageBytes));
@@ -183,14 +183,14 @@ __global__ void __launch_bounds__(kThreads, 1)
         return true;
       };
       auto wait_h = [&]() -> bool {
-        if (!mbar_wait(hready, hw & 1, g.err, 17, abort)) return false;
+        if (!mbar_wait(hready, hw & 1, g.err, 17, abort, g.wait_limit)) return false;
         ++hw;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         return true;
       };
       for (int rb = rb_first; rb <= rb_last && ok; ++rb) {
         const int rbi = rb - rb_first;
-        ok = mbar_wait(afull, rbi & 1, g.err, 18, abort);
+        ok = mbar_wait(afull, rbi & 1, g.err, 18, abort, g.wait_limit);
         if (ok) ok = job(nk1, idesc_bf16(H));               // layer 1 on X
         if (ok) ok = wait_h();                               // h1 in the A region
         if (ok) ok = job(nkh, idesc_bf16(H));               // layer 2 on h1
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     bool ok = true;
     auto wait_full = [&]() -> bool {
       const int a = t & 1;
-      const bool w = __all_sync(0xffffffffu, mbar_wait(tfull0 + 8 * a, (t >> 1) & 1, g.err, 19, abort));
+      const bool w = __all_sync(0xffffffffu, mbar_wait(tfull0 + 8 * a, (t >> 1) & 1, g.err, 19, abort, g.wait_limit));
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       return w;
     };
@@ -411,10 +411,12 @@ cudaError_t mlp_head_argmax(const MlpHeadArgs& a, cudaStream_t st) {
   const int sms = g_num_sms[dev].load(std::memory_order_relaxed);
   const long long tiles = (long long)((a.M + kBM - 1) / kBM) * ((a.N + bn3 - 1) / bn3);
   const dim3 grid((unsigned)(tiles < sms ? tiles : sms));
+  MlpHeadArgs ha = a;
+  ha.wait_limit = wait_limit();
   if (wide)
-    mlp_head_kernel<256><<<grid, kThreads, kSmemBytes, st>>>(mx, m1, m2, m3, a);
+    mlp_head_kernel<256><<<grid, kThreads, kSmemBytes, st>>>(mx, m1, m2, m3, ha);
   else
-    mlp_head_kernel<128><<<grid, kThreads, kSmemBytes, st>>>(mx, m1, m2, m3, a);
+    mlp_head_kernel<128><<<grid, kThreads, kSmemBytes, st>>>(mx, m1, m2, m3, ha);
   return cudaGetLastError();
 }
 

@@ -23,6 +23,7 @@ struct MlpHeadArgs {
   int M, dp, H, N;
   unsigned long long* keys;  // [M], zero on entry
   int* err;                  // device flag: a bounded wait ran out (non-zero code)
+  long long wait_limit;      // try_wait rounds of the pipeline waits (set by the launcher)
   // graph replay: the live row count, read at run time (<= M; the grid and
   // tensor maps are sized for M rows); null for a plain launch
   const int* M_dev = nullptr;

@@ -1,5 +1,6 @@
 // mlp_kernels.cu -- element-wise and reduction kernels of the learned-entry
 // MLP (BF16 storage, FP32 arithmetic).  The GEMMs are gemm_tc.cu.
+#include <algorithm>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -84,13 +85,40 @@ __global__ void relu_grad_k(const float* __restrict__ g, const __nv_bfloat16* __
   out[i] = __float2bfloat16_rn(__bfloat162float(h[i]) > 0.f ? g[i] : 0.f);
 }
 
-// out[n] = sum over m of x[m][n] (BF16 input, FP32 accumulation in row order).
-__global__ void col_sum_bf16_k(const __nv_bfloat16* __restrict__ x, int M, int N,
-                               float* __restrict__ out) {
+// Column sums out[n] = sum over m of x[m][n] (BF16 input, FP32 sums) in two
+// passes with a fixed order, so results are reproducible: block (bx, by)
+// takes columns 32 bx .. 32 bx + 31 and row slice by (rows by*rs ..
+// by*rs + rs - 1); its thread (c, r) sums rows r, r + 8, ... of the slice
+// for column c, the eight row lanes are added in lane order, and
+// part[by][n] receives the slice's sum.  The second pass adds the slices in
+// order.
+constexpr int kColSumRowLanes = 8;
+__global__ void col_sum_part_k(const __nv_bfloat16* __restrict__ x, int M, int N, int rs,
+                               float* __restrict__ part) {
+  __shared__ float sh[kColSumRowLanes][32];
+  const int c = threadIdx.x, r = threadIdx.y;
+  const int n = blockIdx.x * 32 + c;
+  const int m0 = blockIdx.y * rs, m1 = min(M, m0 + rs);
+  float s = 0.f;
+  if (n < N) {
+#pragma unroll 4
+    for (int m = m0 + r; m < m1; m += kColSumRowLanes) s += __bfloat162float(x[(int64_t)m * N + n]);
+  }
+  sh[r][c] = s;
+  __syncthreads();
+  if (r == 0 && n < N) {
+    float t = sh[0][c];
+#pragma unroll
+    for (int i = 1; i < kColSumRowLanes; ++i) t += sh[i][c];
+    part[(int64_t)blockIdx.y * N + n] = t;
+  }
+}
+
+__global__ void col_sum_finish_k(const float* __restrict__ part, int slices, int N, float* __restrict__ out) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
   float s = 0.f;
-  for (int m = 0; m < M; ++m) s += __bfloat162float(x[(int64_t)m * N + n]);
+  for (int i = 0; i < slices; ++i) s += part[(int64_t)i * N + n];
   out[n] = s;
 }
 
@@ -165,8 +193,13 @@ cudaError_t launch_relu_grad(const float* g, const void* h, int64_t n, void* out
   relu_grad_k<<<blocks(n, 256), 256, 0, st>>>(g, (const __nv_bfloat16*)h, n, (__nv_bfloat16*)out);
   return cudaGetLastError();
 }
-cudaError_t launch_col_sum_bf16(const void* x, int M, int N, float* out, cudaStream_t st) {
-  col_sum_bf16_k<<<blocks(N, 128), 128, 0, st>>>((const __nv_bfloat16*)x, M, N, out);
+int col_sum_slices(int M) { return std::max(1, std::min(kColSumMaxSlices, M / 256)); }
+cudaError_t launch_col_sum_bf16(const void* x, int M, int N, float* out, float* part, cudaStream_t st) {
+  const int slices = col_sum_slices(M);
+  const int rs = (M + slices - 1) / slices;
+  col_sum_part_k<<<dim3((N + 31) / 32, slices), dim3(32, kColSumRowLanes), 0, st>>>(
+      (const __nv_bfloat16*)x, M, N, rs, part);
+  col_sum_finish_k<<<blocks(N, 256), 256, 0, st>>>(part, slices, N, out);
   return cudaGetLastError();
 }
 cudaError_t launch_adam(float* w, const float* g, float* m1, float* m2, int64_t n, float lr,

@@ -10,8 +10,9 @@
 // search with every buffer supplied: the caller passes the inputs and the
 // outputs, and the only scratch the two kernels need -- the leaf of each
 // query and the work-queue counter of the persistent search -- lives in the
-// file-scope array below, reserved once when the library is loaded on a
-// device and kept until the process exits.
+// file-scope array below.  The array is reserved on a device when an index
+// is first created there (noalloc_prepare; with lazy module loading the
+// address lookup is what loads it) and kept until the process exits.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -64,6 +65,17 @@ rte_status scratch_for_device(int dev, NoallocScratch** out) {
 
 }  // namespace
 
+namespace rte {
+// Looks up the scratch array's device address for `dev` (the current
+// device).  Index creation calls this, so that the array is allocated -- the
+// lookup loads the module holding it -- when the index is built, not in the
+// middle of the first allocation-free search.
+rte_status noalloc_prepare(int dev) {
+  NoallocScratch* scr = nullptr;
+  return scratch_for_device(dev, &scr);
+}
+}  // namespace rte
+
 extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* projected,
                                                    const int32_t* hits, int64_t nq,
                                                    const rte_search_params* params,
@@ -77,15 +89,9 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
                                 std::to_string(kMaxQueries) + " queries per call");
   if (params->entry_mode != RTE_ENTRY_RANDOM && params->entry_mode != RTE_ENTRY_KDTREE)
     return fail(RTE_EINVAL, "rte_search_projected_noalloc supports random and kd-tree entries only");
-  if (nq == 0) return RTE_OK;
-  if (!projected || !out_ids) return fail(RTE_EINVAL, "NULL argument");
-  // inputs and outputs must already be device memory: copying host data
-  // would need staging buffers
-  if (!is_device_ptr(projected) || !is_device_ptr(out_ids) ||
-      (out_dists && !is_device_ptr(out_dists)) || (hits && !is_device_ptr(hits)))
-    return fail(RTE_EINVAL, "rte_search_projected_noalloc takes device pointers only");
   DeviceGuard guard(x->device);
-  cudaStream_t st = (cudaStream_t)stream;
+  // parameters are validated before an empty batch returns, as
+  // rte_search_projected does
   int L, k, NL, NB, wpb, grid;
   size_t smem;
   rte_status s = search_plan(x, params, nq, &L, &k, &NL, &NB, &wpb, &grid, &smem);
@@ -93,6 +99,14 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   if (params->rerank == 2)
     return fail(RTE_EINVAL, "rerank 2 needs the original queries: use rte_search");
   if (params->max_hits > 1) return fail(RTE_EINVAL, "max_hits > 1 needs rte_search");
+  if (nq == 0) return RTE_OK;
+  if (!projected || !out_ids) return fail(RTE_EINVAL, "NULL argument");
+  // inputs and outputs must already be device memory: copying host data
+  // would need staging buffers
+  if (!is_device_ptr(projected) || !is_device_ptr(out_ids) ||
+      (out_dists && !is_device_ptr(out_dists)) || (hits && !is_device_ptr(hits)))
+    return fail(RTE_EINVAL, "rte_search_projected_noalloc takes device pointers only");
+  cudaStream_t st = (cudaStream_t)stream;
   NoallocScratch* scr = nullptr;
   s = scratch_for_device(x->device, &scr);
   if (s != RTE_OK) return s;

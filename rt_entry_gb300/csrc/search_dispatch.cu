@@ -7,17 +7,20 @@
 
 namespace rte {
 
-void* search_lookup_c1_f32(int, int);
-void* search_lookup_c2_f32(int, int);
-void* search_lookup_c3_f32(int, int);
-void* search_lookup_c3_bf16(int, int);
-void* search_lookup_c3_fp8(int, int);
-void* search_lookup_c4_f32(int, int);
-void* search_lookup_c4_bf16(int, int);
-void* search_lookup_c4_fp8(int, int);
-void* search_lookup_c30_f32(int, int);
-void* search_lookup_c30_bf16(int, int);
-void* search_lookup_c30_fp8(int, int);
+void* search_lookup_c1_f32(int, int, bool);
+void* search_lookup_c2_f32(int, int, bool);
+void* search_lookup_c3_f32(int, int, bool);
+void* search_lookup_c3_bf16(int, int, bool);
+void* search_lookup_c3_fp8(int, int, bool);
+void* search_lookup_c4_f32(int, int, bool);
+void* search_lookup_c4_bf16(int, int, bool);
+void* search_lookup_c4_fp8(int, int, bool);
+void* search_lookup_c30_f32(int, int, bool);
+void* search_lookup_c30_bf16(int, int, bool);
+void* search_lookup_c30_fp8(int, int, bool);
+void* search_lookup_cg_f32(int, int, bool);
+void* search_lookup_cg_bf16(int, int, bool);
+void* search_lookup_cg_fp8(int, int, bool);
 
 namespace {
 struct Entry {
@@ -31,38 +34,52 @@ const Entry kTable[] = {
     {4, search_lookup_c4_f32, search_lookup_c4_bf16, search_lookup_c4_fp8},
     {30, search_lookup_c30_f32, search_lookup_c30_bf16, search_lookup_c30_fp8},
 };
+// Kernels for any chunk count (template C == 0): every other dimension up
+// to 1024, and the precisions a specialised chunk count lacks.
+const Entry kGeneric = {0, search_lookup_cg_f32, search_lookup_cg_bf16, search_lookup_cg_fp8};
+
+KernelLookup pick_prec(const Entry& e, int prec) {
+  return prec == kPrecF32 ? e.f32 : prec == kPrecBF16 ? e.bf16 : prec == kPrecFP8 ? e.fp8 : nullptr;
+}
 }  // namespace
 
-bool search_chunks_supported(int C) {
-  for (const Entry& e : kTable)
-    if (e.C == C) return true;
-  return false;
-}
+bool search_chunks_supported(int C) { return C >= 1 && C <= kMaxChunks; }
 
-void* search_kernel_ptr(int C, int NL, int NB, int prec) {
+int search_kernel_chunks(int C, int NL, int NB, int prec, bool r16) {
   for (const Entry& e : kTable) {
     if (e.C != C) continue;
-    KernelLookup f = prec == kPrecF32 ? e.f32 : prec == kPrecBF16 ? e.bf16 : prec == kPrecFP8 ? e.fp8 : nullptr;
-    return f ? f(NL, NB) : nullptr;
+    KernelLookup f = pick_prec(e, prec);
+    if (f && f(NL, NB, r16)) return C;
   }
-  return nullptr;
+  return 0;
+}
+
+void* search_kernel_ptr(int C, int NL, int NB, int prec, bool r16) {
+  if (!search_chunks_supported(C)) return nullptr;
+  const int kc = search_kernel_chunks(C, NL, NB, prec, r16);
+  const Entry* e = &kGeneric;
+  for (const Entry& t : kTable)
+    if (kc != 0 && t.C == kc) e = &t;
+  KernelLookup f = pick_prec(*e, prec);
+  return f ? f(NL, NB, r16) : nullptr;
 }
 
 cudaError_t launch_search(const SearchArgs& a, int C, int NL, int NB, int prec, int wpb, int grid,
                           size_t smem, cudaStream_t st) {
-  void* k = search_kernel_ptr(C, NL, NB, prec);
+  void* k = search_kernel_ptr(C, NL, NB, prec, a.R == 16);
   if (!k) return cudaErrorInvalidValue;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
   SearchArgs args = a;
+  args.C = C;
   void* params[] = {&args};
   return cudaLaunchKernel(k, dim3(grid), dim3(32 * wpb), params, smem, st);
 }
 
-int occupancy_search(int C, int NL, int NB, int prec, int wpb, size_t smem) {
-  void* k = search_kernel_ptr(C, NL, NB, prec);
+int occupancy_search(int C, int NL, int NB, int prec, bool r16, int wpb, size_t smem) {
+  void* k = search_kernel_ptr(C, NL, NB, prec, r16);
   if (!k) return 0;
   // the answer depends only on (kernel, device, block, shared memory): cache it
   int dev = 0;

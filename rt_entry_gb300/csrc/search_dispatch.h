@@ -9,13 +9,20 @@
 namespace rte {
 
 // Each search_c<C>_<prec>.cu defines one of these; it returns the kernel for
-// (NL, NB) or nullptr when that combination is not instantiated.
-using KernelLookup = void* (*)(int NL, int NB);
+// (NL, NB) over a degree-16 graph (r16) or a graph of degree >= 32, or
+// nullptr when that combination is not instantiated.
+using KernelLookup = void* (*)(int NL, int NB, bool r16);
 
 bool search_chunks_supported(int C);
-void* search_kernel_ptr(int C, int NL, int NB, int prec);
+// The kernel template's C for rows of C chunks, pool registers NL, batch
+// registers NB, a precision and the graph degree (r16: degree 16): C itself where a kernel was built for that
+// combination, else 0 (the kernels built for any chunk count, which keep
+// the query in shared memory).
+int search_kernel_chunks(int C, int NL, int NB, int prec, bool r16);
+void* search_kernel_ptr(int C, int NL, int NB, int prec, bool r16);
+// The degree comes from a.R (16 selects the degree-16 kernels).
 cudaError_t launch_search(const SearchArgs& a, int C, int NL, int NB, int prec, int wpb, int grid,
                           size_t smem, cudaStream_t st);
-int occupancy_search(int C, int NL, int NB, int prec, int wpb, size_t smem);
+int occupancy_search(int C, int NL, int NB, int prec, bool r16, int wpb, size_t smem);
 
 }  // namespace rte

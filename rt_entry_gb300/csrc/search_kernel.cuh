@@ -138,6 +138,14 @@ __device__ __forceinline__ void cx_regs(float& da, int& ia, float& db, int& ib, 
 // register keep (MAX, np) padding that no step ever reads back.
 __host__ __device__ constexpr int pool_slots(int NL) { return NL == 0 ? 16 : 32 * NL; }
 __host__ __device__ constexpr int pool_regs(int NL) { return NL == 0 ? 1 : NL; }
+// Batch geometry: NB registers of 32 slots, or NB == 0 for a 16-slot batch
+// (search width 1 over a degree-16 graph) in lanes 0..15 of one register;
+// lanes 16..31 then hold (MAX, np) padding.
+__host__ __device__ constexpr int batch_slots(int NB) { return NB == 0 ? 16 : 32 * NB; }
+__host__ __device__ constexpr int batch_regs(int NB) { return NB == 0 ? 1 : NB; }
+// Query registers per lane: C, or one unused register for the kernels built
+// for any chunk count (C == 0), which keep the query in shared memory.
+__host__ __device__ constexpr int qregs(int C) { return C == 0 ? 1 : C; }
 
 // Bitonic sort of N slots (graph_search.cuh:888-919), N = 32*NB by default or
 // 16 for the one-register beam-16 pool.  With DESC_FINAL the pair (a, a+sub)
@@ -179,9 +187,41 @@ __device__ __forceinline__ void sort_batch_desc(float (&d)[NB], int (&id)[NB], i
 // are in the same lane.  The main loop skips a batch slot holding MAX.
 template <int NL, int NB>
 __device__ __forceinline__ void merge_pool(float (&pd)[pool_regs(NL)], int (&pi)[pool_regs(NL)],
-                                           const float (&bd)[NB], const int (&bi)[NB], bool skip_max,
-                                           int lane) {
-  if constexpr (NL == 0) {
+                                           const float (&bd)[batch_regs(NB)],
+                                           const int (&bi)[batch_regs(NB)], bool skip_max, int lane) {
+  if constexpr (NB == 0) {
+    // 16-slot batch: n = 16, batch slot i (lane i) meets pool slot L-16+i,
+    // which is lane i of a 16-slot pool or lane 16+i of the last register
+    float od = bd[0];
+    int oi = bi[0];
+    if constexpr (NL != 0) {
+      od = __shfl_up_sync(kFull, od, 16);
+      oi = __shfl_up_sync(kFull, oi, 16);
+    }
+    constexpr int PR = pool_regs(NL);
+    const bool mine = NL == 0 ? lane < 16 : lane >= 16;
+    bool take = mine && pd[PR - 1] > od;
+    if (skip_max && od == kMaxDist) take = false;
+    if (take) {
+      pd[PR - 1] = od;
+      pi[PR - 1] = oi;
+    }
+    constexpr int L = pool_slots(NL);
+#pragma unroll
+    for (int sub = L / 2; sub >= 1; sub >>= 1) {
+      if (sub >= 32) {
+        const int rs = sub >> 5;
+#pragma unroll
+        for (int j = 0; j < PR; ++j) {
+          if (j & rs) continue;
+          cx_regs(pd[j], pi[j], pd[j + rs], pi[j + rs], false);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < PR; ++j) cx_lanes(pd[j], pi[j], sub, false, lane);
+      }
+    }
+  } else if constexpr (NL == 0) {
     // 16-slot pool: pool slot i (lane i) meets batch slot B-16+i, which is
     // lane 16+i of the last batch register.
     const float od = __shfl_down_sync(kFull, bd[NB - 1], 16);
@@ -234,11 +274,12 @@ __device__ __forceinline__ void merge_pool(float (&pd)[pool_regs(NL)], int (&pi)
 // therefore leaves the pool unchanged, ids and order included, and
 // search_query skips both.
 template <int NL, int NB>
-__device__ __forceinline__ bool batch_can_enter(const float (&pd)[pool_regs(NL)], const float (&bd)[NB]) {
+__device__ __forceinline__ bool batch_can_enter(const float (&pd)[pool_regs(NL)],
+                                                const float (&bd)[batch_regs(NB)]) {
   const float pmax = __shfl_sync(kFull, pd[pool_regs(NL) - 1], NL == 0 ? 15 : 31);
   bool below = false;
 #pragma unroll
-  for (int j = 0; j < NB; ++j) below |= bd[j] < pmax;
+  for (int j = 0; j < batch_regs(NB); ++j) below |= bd[j] < pmax;
   return __any_sync(kFull, below);
 }
 
@@ -301,8 +342,14 @@ __device__ __forceinline__ float lane_partial(const float (&p)[C], const float (
 // positions, so each k pairs the base and query values of one dimension.
 // With integer-valued data of magnitude < 2^8 every term is exact and the
 // distances equal the FP32 path's bit for bit.
-template <int C, int PREC, bool MMA = (PREC == kPrecBF16 && C <= 4)>
+template <int C, int PREC, bool MMA = (PREC == kPrecBF16 && C >= 1 && C <= 4)>
 struct QueryExtra {};
+// Kernels for any chunk count (C == 0): the FP32 query row in the warp's
+// shared memory, in the base rows' interleaved layout.
+template <int PREC>
+struct QueryExtra<0, PREC, false> {
+  const float* qs;
+};
 template <int C, int PREC>
 struct QueryExtra<C, PREC, true> {
   const uint32_t* qs;  // the query's BF16 row in the warp's shared memory (16*C words)
@@ -392,6 +439,165 @@ __device__ __forceinline__ void distances_mma(const SearchArgs& a, const QueryEx
   }
 }
 
+// ---- rows of a run-time chunk count (kernels built for any dimension) ----
+// A row of C chunks is streamed slab by slab in the interleaved layout
+// (layout.cuh): chunks 4s..4s+3 as one 4-value load per lane, then a pair,
+// then a single chunk.  Each value is widened to FP32 (BF16 exactly; FP8
+// times the row's scale) before the subtraction, as RowLoader does.
+template <int PREC>
+struct SlabLoader;
+
+template <>
+struct SlabLoader<kPrecF32> {
+  static constexpr int kBytes = 4;
+  const float* row;
+  __device__ __forceinline__ void init(const SearchArgs& a, int id, size_t stride) { row = a.base + (size_t)id * stride; }
+  __device__ __forceinline__ float4 quad(int off, int lane) const {
+    return __ldg(reinterpret_cast<const float4*>(row + off) + lane);
+  }
+  __device__ __forceinline__ float2 pair(int off, int lane) const {
+    return __ldg(reinterpret_cast<const float2*>(row + off) + lane);
+  }
+  __device__ __forceinline__ float one(int off, int lane) const { return __ldg(row + off + lane); }
+};
+
+template <>
+struct SlabLoader<kPrecBF16> {
+  static constexpr int kBytes = 2;
+  const uint16_t* row;
+  __device__ __forceinline__ void init(const SearchArgs& a, int id, size_t stride) {
+    row = a.base_bf16 + (size_t)id * stride;
+  }
+  __device__ __forceinline__ float4 quad(int off, int lane) const {
+    const uint2 x = __ldg(reinterpret_cast<const uint2*>(row + off) + lane);
+    return make_float4(bf16lo(x.x), bf16hi(x.x), bf16lo(x.y), bf16hi(x.y));
+  }
+  __device__ __forceinline__ float2 pair(int off, int lane) const {
+    const uint32_t y = __ldg(reinterpret_cast<const unsigned int*>(row + off) + lane);
+    return make_float2(bf16lo(y), bf16hi(y));
+  }
+  __device__ __forceinline__ float one(int off, int lane) const {
+    return __uint_as_float((uint32_t)__ldg(row + off + lane) << 16);
+  }
+};
+
+template <>
+struct SlabLoader<kPrecFP8> {
+  static constexpr int kBytes = 1;
+  const uint8_t* row;
+  float sc;
+  __device__ __forceinline__ void init(const SearchArgs& a, int id, size_t stride) {
+    row = a.base_fp8 + (size_t)id * stride;
+    sc = __ldg(a.fp8_scale + id);
+  }
+  __device__ __forceinline__ float4 quad(int off, int lane) const {
+    const uint32_t x = __ldg(reinterpret_cast<const unsigned int*>(row + off) + lane);
+    const float2 u = fp8x2_to_float2((uint16_t)(x & 0xffffu));
+    const float2 v = fp8x2_to_float2((uint16_t)(x >> 16));
+    return make_float4(__fmul_rn(u.x, sc), __fmul_rn(u.y, sc), __fmul_rn(v.x, sc), __fmul_rn(v.y, sc));
+  }
+  __device__ __forceinline__ float2 pair(int off, int lane) const {
+    const float2 u = fp8x2_to_float2(__ldg(reinterpret_cast<const unsigned short*>(row + off) + lane));
+    return make_float2(__fmul_rn(u.x, sc), __fmul_rn(u.y, sc));
+  }
+  __device__ __forceinline__ float one(int off, int lane) const {
+    return __fmul_rn(fp8x2_to_float2((uint16_t)__ldg(row + off + lane)).x, sc);
+  }
+};
+
+// One chunk of a lane's partial: fmaf(t, t, s) with t = p - q.  The first
+// chunk starts from s = +0, and fmaf(t, t, +0) rounds exactly as t * t, so
+// the sum equals lane_partial's.
+__device__ __forceinline__ float chunk_acc(float p, float q, float s) {
+  const float t = __fsub_rn(p, q);
+  return __fmaf_rn(t, t, s);
+}
+
+// The butterfly reduction of G rows' lane partials (see `distances`): row
+// g0 + lane / (32/G) is complete in the first lane of each 32/G-lane span.
+template <int G>
+__device__ __forceinline__ void reduce_rows(float (&part)[G], float* s_dist, int g0, int n, int lane) {
+  constexpr int SPAN = 32 / G;
+#pragma unroll
+  for (int off = 16, half = G / 2; half >= 1; off >>= 1, half >>= 1) {
+    const bool up = (lane & off) != 0;
+#pragma unroll
+    for (int t = 0; t < half; ++t) {
+      float send = up ? part[t] : part[t + half];
+      float keep = up ? part[t + half] : part[t];
+      part[t] = __fadd_rn(keep, __shfl_xor_sync(kFull, send, off));
+    }
+  }
+  float total = part[0];
+#pragma unroll
+  for (int off = SPAN / 2; off >= 1; off >>= 1) total = __fadd_rn(total, __shfl_xor_sync(kFull, total, off));
+  const int row = g0 + lane / SPAN;
+  if ((lane % SPAN) == 0 && row < n) s_dist[row] = total;
+}
+
+// Distances of n rows of a.C chunks against the query row in shared memory
+// qs (interleaved layout), G rows in flight.
+template <int PREC>
+__device__ __forceinline__ void distances_rt(const SearchArgs& a, const float* qs, const int* s_ids,
+                                             float* s_dist, int n, int lane) {
+  constexpr int G = 4;
+  const int C = a.C, n4 = C >> 2, rem = C & 3;
+  const size_t stride = 32 * (size_t)C;  // elements per row
+  {
+    const int lines = (int)((stride * SlabLoader<PREC>::kBytes + 127) / 128);
+    const char* rows = PREC == kPrecF32    ? reinterpret_cast<const char*>(a.base)
+                       : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
+                                           : reinterpret_cast<const char*>(a.base_fp8);
+    const size_t rb = stride * SlabLoader<PREC>::kBytes;
+    for (int i = lane; i < n * lines; i += 32) {
+      const int row = i / lines, line = i - row * lines;
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(rows + (size_t)s_ids[row] * rb + line * 128));
+    }
+  }
+  for (int g0 = 0; g0 < n; g0 += G) {
+    SlabLoader<PREC> r[G];
+#pragma unroll
+    for (int t = 0; t < G; ++t) r[t].init(a, s_ids[g0 + t < n ? g0 + t : g0], stride);
+    float part[G];
+#pragma unroll
+    for (int t = 0; t < G; ++t) part[t] = 0.0f;
+#pragma unroll 2
+    for (int sl = 0; sl < n4; ++sl) {
+      const float4 q = *reinterpret_cast<const float4*>(qs + 128 * sl + 4 * lane);
+      float4 v[G];
+#pragma unroll
+      for (int t = 0; t < G; ++t) v[t] = r[t].quad(128 * sl, lane);
+#pragma unroll
+      for (int t = 0; t < G; ++t) {
+        part[t] = chunk_acc(v[t].x, q.x, part[t]);
+        part[t] = chunk_acc(v[t].y, q.y, part[t]);
+        part[t] = chunk_acc(v[t].z, q.z, part[t]);
+        part[t] = chunk_acc(v[t].w, q.w, part[t]);
+      }
+    }
+    int off = 128 * n4;
+    if (rem >= 2) {
+      const float2 q = *reinterpret_cast<const float2*>(qs + off + 2 * lane);
+#pragma unroll
+      for (int t = 0; t < G; ++t) {
+        const float2 v = r[t].pair(off, lane);
+        part[t] = chunk_acc(v.x, q.x, part[t]);
+        part[t] = chunk_acc(v.y, q.y, part[t]);
+      }
+      off += 64;
+    }
+    if (rem & 1) {
+      const float q = qs[off + lane];
+#pragma unroll
+      for (int t = 0; t < G; ++t) part[t] = chunk_acc(r[t].one(off, lane), q, part[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < G; ++t)
+      if (g0 + t >= n) part[t] = 0.0f;
+    reduce_rows<G>(part, s_dist, g0, n, lane);
+  }
+}
+
 // Distances of the n (<= B) ids in s_ids[0..n) written to s_dist[0..n).
 // Groups of G rows (16, or 8 for long rows): each lane forms its partial for
 // the G rows; a butterfly over offsets 16, 8, ... exchanges half of the rows
@@ -400,61 +606,50 @@ __device__ __forceinline__ void distances_mma(const SearchArgs& a, const QueryEx
 // Every addition pairs the same two partial sums as the reference's
 // shuffle-down tree (addition is commutative, so the results are equal).
 template <int C, int PREC>
-__device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)[C],
+__device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)[qregs(C)],
                                           const QueryExtra<C, PREC>& qx, const int* s_ids,
                                           float* s_dist, int n, int lane) {
-  if constexpr (PREC == kPrecBF16 && C <= 4) {
+  if constexpr (C == 0) {
+    distances_rt<PREC>(a, qx.qs, s_ids, s_dist, n, lane);
+  } else if constexpr (PREC == kPrecBF16 && C <= 4) {
     distances_mma<C>(a, qx, s_ids, s_dist, n, lane);
-    return;
-  }
-  constexpr int G = C <= 4 ? 8 : 2;
-  constexpr int SPAN = 32 / G;  // lanes sharing one row after the butterfly
-  {
-    constexpr int kRowBytes = 32 * C * (PREC == kPrecF32 ? 4 : PREC == kPrecBF16 ? 2 : 1);
-    const char* rows = PREC == kPrecF32    ? reinterpret_cast<const char*>(a.base)
-                       : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
-                                           : reinterpret_cast<const char*>(a.base_fp8);
-    prefetch_rows<kRowBytes>(rows, s_ids, n, lane);
-  }
-  for (int g0 = 0; g0 < n; g0 += G) {
-    // all G loads first, unconditionally (a short group re-reads its first
-    // row), so they are issued back to back before any use
-    RowLoader<C, PREC> r[G];
-#pragma unroll
-    for (int t = 0; t < G; ++t) r[t].load(a, s_ids[g0 + t < n ? g0 + t : g0], lane);
-    float part[G];
-#pragma unroll
-    for (int t = 0; t < G; ++t) part[t] = g0 + t < n ? lane_partial<C>(r[t].v, qv) : 0.0f;
-#pragma unroll
-    for (int off = 16, half = G / 2; half >= 1; off >>= 1, half >>= 1) {
-      const bool up = (lane & off) != 0;
-#pragma unroll
-      for (int t = 0; t < half; ++t) {
-        float send = up ? part[t] : part[t + half];
-        float keep = up ? part[t + half] : part[t];
-        part[t] = __fadd_rn(keep, __shfl_xor_sync(kFull, send, off));
-      }
+  } else {
+    constexpr int G = C <= 4 ? 8 : 2;
+    {
+      constexpr int kRowBytes = 32 * C * (PREC == kPrecF32 ? 4 : PREC == kPrecBF16 ? 2 : 1);
+      const char* rows = PREC == kPrecF32    ? reinterpret_cast<const char*>(a.base)
+                         : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
+                                             : reinterpret_cast<const char*>(a.base_fp8);
+      prefetch_rows<kRowBytes>(rows, s_ids, n, lane);
     }
-    float total = part[0];
+    for (int g0 = 0; g0 < n; g0 += G) {
+      // all G loads first, unconditionally (a short group re-reads its first
+      // row), so they are issued back to back before any use
+      RowLoader<C, PREC> r[G];
 #pragma unroll
-    for (int off = SPAN / 2; off >= 1; off >>= 1) total = __fadd_rn(total, __shfl_xor_sync(kFull, total, off));
-    const int row = g0 + lane / SPAN;
-    if ((lane % SPAN) == 0 && row < n) s_dist[row] = total;
+      for (int t = 0; t < G; ++t) r[t].load(a, s_ids[g0 + t < n ? g0 + t : g0], lane);
+      float part[G];
+#pragma unroll
+      for (int t = 0; t < G; ++t) part[t] = g0 + t < n ? lane_partial<C>(r[t].v, qv) : 0.0f;
+      reduce_rows<G>(part, s_dist, g0, n, lane);
+    }
   }
 }
 
 // Compact the valid batch ids (0 <= id < np) into s_ids in slot order,
 // compute their distances, and scatter them back (invalid slots -> MAX).
 template <int C, int NB, int PREC>
-__device__ __forceinline__ int batch_distances(const SearchArgs& a, const float (&qv)[C],
-                                               const QueryExtra<C, PREC>& qx, float (&bd)[NB],
-                                               const int (&bi)[NB], int* s_ids, float* s_dist,
-                                               int lane) {
+__device__ __forceinline__ int batch_distances(const SearchArgs& a, const float (&qv)[qregs(C)],
+                                               const QueryExtra<C, PREC>& qx,
+                                               float (&bd)[batch_regs(NB)],
+                                               const int (&bi)[batch_regs(NB)], int* s_ids,
+                                               float* s_dist, int lane) {
+  constexpr int BR = batch_regs(NB);
   const unsigned lt = (1u << lane) - 1u;
-  int kidx[NB];
+  int kidx[BR];
   int n = 0;
 #pragma unroll
-  for (int j = 0; j < NB; ++j) {
+  for (int j = 0; j < BR; ++j) {
     const bool v = bi[j] >= 0 && bi[j] < a.np;
     const unsigned m = __ballot_sync(kFull, v);
     kidx[j] = v ? n + __popc(m & lt) : -1;
@@ -465,7 +660,7 @@ __device__ __forceinline__ int batch_distances(const SearchArgs& a, const float 
   distances<C, PREC>(a, qv, qx, s_ids, s_dist, n, lane);
   __syncwarp();
 #pragma unroll
-  for (int j = 0; j < NB; ++j) bd[j] = kidx[j] >= 0 ? s_dist[kidx[j]] : kMaxDist;
+  for (int j = 0; j < BR; ++j) bd[j] = kidx[j] >= 0 ? s_dist[kidx[j]] : kMaxDist;
   __syncwarp();
   return n;
 }
@@ -477,9 +672,10 @@ __device__ __forceinline__ int batch_distances(const SearchArgs& a, const float 
 // The reference's precedent is the host-side parallel_reorder
 // (graph_helper.cu:146-213), which recomputes FP32 L2 and std::sorts.
 template <int C, int NL>
-__device__ __forceinline__ void rerank_pool(const SearchArgs& a, const float (&qv)[C],
-                                            float (&pd)[pool_regs(NL)], int (&pi)[pool_regs(NL)],
-                                            int* s_ids, float* s_dist, int lane) {
+__device__ __forceinline__ void rerank_pool(const SearchArgs& a, const float (&qv)[qregs(C)],
+                                            const float* qsm, float (&pd)[pool_regs(NL)],
+                                            int (&pi)[pool_regs(NL)], int* s_ids, float* s_dist,
+                                            int lane) {
   constexpr int PR = pool_regs(NL);
   const unsigned lt = (1u << lane) - 1u;
   int kidx[PR];
@@ -494,7 +690,9 @@ __device__ __forceinline__ void rerank_pool(const SearchArgs& a, const float (&q
     n += __popc(m);
   }
   __syncwarp();
-  distances<C, kPrecF32>(a, qv, QueryExtra<C, kPrecF32>{}, s_ids, s_dist, n, lane);
+  QueryExtra<C, kPrecF32> q32{};
+  if constexpr (C == 0) q32.qs = qsm;
+  distances<C, kPrecF32>(a, qv, q32, s_ids, s_dist, n, lane);
   __syncwarp();
 #pragma unroll
   for (int j = 0; j < PR; ++j) pd[j] = kidx[j] >= 0 ? s_dist[kidx[j]] : kMaxDist;
@@ -502,25 +700,46 @@ __device__ __forceinline__ void rerank_pool(const SearchArgs& a, const float (&q
   sort_batch_desc<PR, false, pool_slots(NL)>(pd, pi, lane);
 }
 
-template <int C, int NL, int NB, int PREC>
+// One query.  Batch slot p (lane p % 32 of register p / 32) belongs to the
+// (p / R)-th node selected in the iteration and holds entry p % R of its
+// neighbour list.  For R >= 32 a node's list fills R / 32 whole registers
+// (register j holds node j / (R / 32)); R16 kernels serve degree-16 graphs,
+// whose lists fill half a register (slot p holds node p / 16).
+template <int C, int NL, int NB, int PREC, bool R16>
 __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& bloom, int* s_ids,
                              float* s_dist, uint32_t* q_slot) {
   constexpr int L = pool_slots(NL);
   constexpr int PR = pool_regs(NL);  // pool registers
-  // the merge reads batch registers NB - min(PR, NB) .. NB-1 only
-  constexpr int kMergeFrom = NB - (PR < NB ? PR : NB);
-  constexpr int B = 32 * NB;
+  constexpr int BR = batch_regs(NB);  // batch registers
+  // the merge reads batch registers BR - min(PR, BR) .. BR-1 only
+  constexpr int kMergeFrom = BR - (PR < BR ? PR : BR);
+  constexpr int B = batch_slots(NB);
+  static_assert(R16 || NB > 0, "a 16-slot batch comes from a degree-16 graph");
   const int np = a.np;
-  const int R = a.R;
-  const int NR = R >> 5;  // batch registers per expanded node
-  const int nr_shift = __ffs(NR) - 1;  // R is a power of two >= 32: j / NR == j >> nr_shift
+  const int R = R16 ? 16 : a.R;
+  const int NR = R >> 5;               // batch registers per node (R >= 32)
+  const int nr_shift = __ffs(NR) - 1;  // j / NR == j >> nr_shift
   int c_entries = 0, c_expanded = 0, c_dists = 0;  // per query: far below 2^31
 
-  float qv[C];
+  float qv[qregs(C)];
+  QueryExtra<C, PREC> qx;
+  if constexpr (C == 0) {
+    // the query row in the warp's shared memory, interleaved like the base
+    float* qs = reinterpret_cast<float*>(q_slot);
+    for (int c = 0; c < a.C; ++c) {
+      const int dim = lane + 32 * c;
+      qs[interleaved_offset(c, lane, a.C)] = dim < a.d ? __ldg(a.queries + (size_t)q * a.qstride + dim) : 0.0f;
+    }
+    qv[0] = 0.0f;
+    qx.qs = qs;
+    __syncwarp();
+  } else {
 #pragma unroll
-  for (int c = 0; c < C; ++c) {
-    const int dim = lane + 32 * c;
-    qv[c] = dim < a.d ? __ldg(a.queries + (size_t)q * a.qstride + dim) : 0.0f;
+    for (int c = 0; c < C; ++c) {
+      const int dim = lane + 32 * c;
+      qv[c] = dim < a.d ? __ldg(a.queries + (size_t)q * a.qstride + dim) : 0.0f;
+    }
+    if constexpr (PREC == kPrecBF16 && C <= 4) make_query_extra<C>(qx, qv, q_slot, lane);
   }
 
   float pd[PR];
@@ -530,11 +749,8 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     pd[j] = kMaxDist;
     pi[j] = np;
   }
-  float bd[NB];
-  int bi[NB];
-
-  QueryExtra<C, PREC> qx;
-  if constexpr (PREC == kPrecBF16 && C <= 4) make_query_extra<C>(qx, qv, q_slot, lane);
+  float bd[BR];
+  int bi[BR];
 
   bloom.clear(lane);
   __syncwarp();
@@ -565,10 +781,11 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
 #pragma unroll 1
   for (int it = 0; it < n_ebatch; ++it) {
 #pragma unroll
-    for (int j = 0; j < NB; ++j) {
-      const int pos = it * B + (j << 5) + lane;
+    for (int j = 0; j < BR; ++j) {
+      const int slot = (j << 5) + lane;
+      const int pos = it * B + slot;
       int id = np;
-      if (pos < n_entries) {
+      if (slot < B && pos < n_entries) {
         if (a.entry_mode == 0) {
           uint32_t& s = (j & 1) ? seed1 : seed0;
           s = s * 1103515245u + 12345u;
@@ -589,7 +806,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     __syncwarp();
     c_entries += batch_distances<C, NB, PREC>(a, qv, qx, bd, bi, s_ids, s_dist, lane);
     if (batch_can_enter<NL, NB>(pd, bd)) {
-      sort_batch_desc<NB, true, 32 * NB, kMergeFrom>(bd, bi, lane);
+      sort_batch_desc<BR, true, B, kMergeFrom>(bd, bi, lane);
       merge_pool<NL, NB>(pd, pi, bd, bi, false, lane);
     }
   }
@@ -619,8 +836,11 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
   while (iter < a.max_iter) {
     iter++;
     // select up to W unvisited pool slots in pool order; mark them visited by
-    // negating the id (:986-1031)
-    int nodes[NB];
+    // negating the id (:986-1031).  nodes[s]: the s-th selected node (R >=
+    // 32); slot_node[j]: the node whose list fills this lane's slot of batch
+    // register j (R16).
+    int nodes[R16 ? 1 : BR];
+    int slot_node[R16 ? BR : 1];
     int nsel = 0;
 #pragma unroll 1
     while (nsel < a.W && tmp_flag != 0) {
@@ -634,9 +854,16 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
       }
       tmp_flag &= ~(1u << pos);
       const int node = v < 0 ? -v : v;
+      if constexpr (R16) {
 #pragma unroll
-      for (int s = 0; s < NB; ++s)
-        if (s == nsel) nodes[s] = node;
+        for (int j = 0; j < BR; ++j)
+          if ((((j << 5) + lane) >> 4) == nsel) slot_node[j] = node;
+        if (lane == 0) c_expanded += node < np ? 1 : 0;
+      } else {
+#pragma unroll
+        for (int s = 0; s < BR; ++s)
+          if (s == nsel) nodes[s] = node;
+      }
       nsel++;
       if (nsel == a.W) break;
       while (tmp_flag == 0 && iteration < PR) {
@@ -649,43 +876,74 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     // neighbour rows of the selected nodes (:995-1010); a node id >= np
     // expands nothing (the reference would read past the graph)
 #pragma unroll
-    for (int j = 0; j < NB; ++j) {
-      const int s = j >> nr_shift;
+    for (int j = 0; j < BR; ++j) {
       int id = np;
-      if (s < nsel) {
-        const int node = pick<NB>(nodes, s);
-        if (node < np) id = __ldg(a.graph + (size_t)node * R + ((j - s * NR) << 5) + lane);
+      if constexpr (R16) {
+        const int slot = (j << 5) + lane;
+        if (slot < B && (slot >> 4) < nsel) {
+          const int node = slot_node[j];
+          if (node < np) id = __ldg(a.graph + (size_t)node * 16 + (slot & 15));
+        }
+      } else {
+        const int s = j >> nr_shift;
+        if (s < nsel) {
+          const int node = pick<BR>(nodes, s);
+          if (node < np) id = __ldg(a.graph + (size_t)node * R + ((j - s * NR) << 5) + lane);
+        }
       }
       bi[j] = id;
     }
+    // canonical rule: every test of one list sees the filter before any add
+    // of that list; lists in selection order
+    if constexpr (R16) {
+#pragma unroll 1
+      for (int s = 0; s < nsel; ++s) {
+        bool pass[BR];
 #pragma unroll
-    for (int s = 0; s < NB; ++s) {
-      if (s >= nsel) break;
-      if (lane == 0) c_expanded += pick<NB>(nodes, s) < np ? 1 : 0;
-      // canonical rule: every test of one list sees the filter before any
-      // add of that list; lists in selection order
-      bool pass[NB];
-#pragma unroll
-      for (int j = 0; j < NB; ++j) {
-        pass[j] = false;
-        if ((j >> nr_shift) == s) pass[j] = bi[j] != np && !bloom.test((uint32_t)bi[j]);
-      }
-      __syncwarp();
-#pragma unroll
-      for (int j = 0; j < NB; ++j) {
-        if ((j >> nr_shift) == s) {
-          if (pass[j])
-            bloom.add((uint32_t)bi[j]);
-          else
-            bi[j] = np;
+        for (int j = 0; j < BR; ++j) {
+          pass[j] = false;
+          if ((((j << 5) + lane) >> 4) == s) pass[j] = bi[j] != np && !bloom.test((uint32_t)bi[j]);
         }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < BR; ++j) {
+          if ((((j << 5) + lane) >> 4) == s) {
+            if (pass[j])
+              bloom.add((uint32_t)bi[j]);
+            else
+              bi[j] = np;
+          }
+        }
+        __syncwarp();
       }
-      __syncwarp();
+    } else {
+#pragma unroll
+      for (int s = 0; s < BR; ++s) {
+        if (s >= nsel) break;
+        if (lane == 0) c_expanded += pick<BR>(nodes, s) < np ? 1 : 0;
+        bool pass[BR];
+#pragma unroll
+        for (int j = 0; j < BR; ++j) {
+          pass[j] = false;
+          if ((j >> nr_shift) == s) pass[j] = bi[j] != np && !bloom.test((uint32_t)bi[j]);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < BR; ++j) {
+          if ((j >> nr_shift) == s) {
+            if (pass[j])
+              bloom.add((uint32_t)bi[j]);
+            else
+              bi[j] = np;
+          }
+        }
+        __syncwarp();
+      }
     }
 
     c_dists += batch_distances<C, NB, PREC>(a, qv, qx, bd, bi, s_ids, s_dist, lane);
     if (batch_can_enter<NL, NB>(pd, bd)) {
-      sort_batch_desc<NB, true, 32 * NB, kMergeFrom>(bd, bi, lane);
+      sort_batch_desc<BR, true, B, kMergeFrom>(bd, bi, lane);
       merge_pool<NL, NB>(pd, pi, bd, bi, true, lane);
     }
 
@@ -715,7 +973,8 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
   }
 
   // ---- exact FP32 rerank of the final pool (precision paths) ----
-  if (PREC != kPrecF32 && a.rerank) rerank_pool<C, NL>(a, qv, pd, pi, s_ids, s_dist, lane);
+  if (PREC != kPrecF32 && a.rerank)
+    rerank_pool<C, NL>(a, qv, reinterpret_cast<const float*>(q_slot), pd, pi, s_ids, s_dist, lane);
 
   // ---- output (:1959-1963) ----
 #pragma unroll
@@ -735,14 +994,16 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
   }
 }
 
-template <int C, int NL, int NB, int PREC>
+template <int C, int NL, int NB, int PREC, bool R16 = false>
 __global__ void __launch_bounds__(256, (C <= 4 ? 4 : 2)) search_kernel(SearchArgs a) {
   extern __shared__ uint32_t smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  constexpr int B = 32 * NB;
+  constexpr int B = batch_slots(NB);
   constexpr int S = B > pool_slots(NL) ? B : pool_slots(NL);  // compaction slots per warp
-  const int per_warp = a.bloom_words + 2 * S + kQuerySlotWords;
+  int qwords = kQuerySlotWords;
+  if constexpr (C == 0) qwords = query_slot_words_for(0, a.C);
+  const int per_warp = a.bloom_words + 2 * S + qwords;
   uint32_t* wbase = smem + (size_t)wib * per_warp;
   Bloom bloom;
   bloom.w = wbase;
@@ -758,8 +1019,8 @@ __global__ void __launch_bounds__(256, (C <= 4 ? 4 : 2)) search_kernel(SearchArg
     if (lane == 0) q = (int)atomicAdd(a.work, 1u);
     q = __shfl_sync(kFull, q, 0);
     if (q >= nq) break;
-    search_query<C, NL, NB, PREC>(a, q, lane, bloom, s_ids, s_dist,
-                                  reinterpret_cast<uint32_t*>(s_dist + S));
+    search_query<C, NL, NB, PREC, R16>(a, q, lane, bloom, s_ids, s_dist,
+                                       reinterpret_cast<uint32_t*>(s_dist + S));
   }
 }
 

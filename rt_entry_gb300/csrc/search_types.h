@@ -6,11 +6,23 @@ namespace rte {
 
 enum : int { kPrecF32 = 0, kPrecBF16 = 1, kPrecFP8 = 2 };
 
+#ifdef __CUDACC__
+#define RTE_HD __host__ __device__
+#else
+#define RTE_HD
+#endif
+
 // Shared memory of one warp of the search kernel, in 32-bit words: the bloom
-// filter, 2*max(batch, beam) compaction slots, and a slot for the query's
-// BF16 row (tensor-core distances, up to 128 dims).
+// filter, 2*max(batch, beam) compaction slots, and a slot for the query:
+// its BF16 row (tensor-core distances, up to 128 dims) in the kernels built
+// for one chunk count, or its FP32 row of `chunks` chunks in the kernels
+// built for any chunk count (kernel template C == 0).
 constexpr int kQuerySlotWords = 64;
+RTE_HD constexpr int query_slot_words_for(int C, int chunks) {
+  return C == 0 ? (32 * chunks > kQuerySlotWords ? 32 * chunks : kQuerySlotWords) : kQuerySlotWords;
+}
 constexpr int kMaxHits = 8;  // leaves per query for kd-tree entries
+constexpr int kMaxChunks = 32;  // rows of up to 1024 dims
 
 struct SearchArgs {
   const float* base;        // lane-interleaved FP32 rows, stride 32*C floats
@@ -32,6 +44,7 @@ struct SearchArgs {
   int n_leaves;             // hits outside [0, n_leaves) fall back to leaf 0
   int max_hits;             // entry mode 1: hits holds [nq][max_hits] leaves (-1 padded)
   const int* nq_dev;        // if set, the query count is read here (graph replay)
+  int C;                    // chunks of 32 dims per row (set by launch_search)
 };
 
 }  // namespace rte

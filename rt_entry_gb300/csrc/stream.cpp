@@ -94,7 +94,7 @@ rte_status capture(rte_batcher* b) {
     work = b->dzero.p + b->cap * 2 + 1;
     e = launch_project_bf16_dyn(b->dq.p, b->cap, b->dn.p, x->dim, x->dim, x->d_mean.p, x->d_rot.p,
                                 x->search_dim, x->search_dim, b->dproj.p, x->search_dim, b->dxb.p,
-                                x->mlp.in_scale, x->mlp.dp, b->dzero.p, zwords, st);
+                                x->mlp.in_scale, x->mlp.dp, b->dzero.p, zwords, st, x->d_rot_split.p);
     qp = b->dproj.p;
     // the kd-tree leaf on a parallel branch
     if (e == cudaSuccess) e = cudaEventRecord(b->fork, st);
@@ -132,7 +132,8 @@ rte_status capture(rte_batcher* b) {
     e = cudaMemsetAsync(b->dwork.p, 0, sizeof(unsigned int), st);
     if (e == cudaSuccess && x->has_pca) {
       e = launch_project_dyn(b->dq.p, b->cap, b->dn.p, x->dim, x->dim, x->d_mean.p, x->d_rot.p,
-                             x->search_dim, x->search_dim, b->dproj.p, x->search_dim, st);
+                             x->search_dim, x->search_dim, b->dproj.p, x->search_dim, st,
+                             x->d_rot_split.p);
       qp = b->dproj.p;
     }
     if (e == cudaSuccess && b->prm.entry_mode == RTE_ENTRY_KDTREE)

@@ -9,7 +9,16 @@
 namespace rte {
 namespace tc {
 
-constexpr long long kWaitLimit = 1ll << 24;  // try_wait rounds before giving up (~seconds)
+// try_wait rounds before a bounded wait gives up (~seconds).  Pipeline waits
+// take their limit from the launch arguments (rte_set_wait_limit lowers it
+// for tests); the waits that let copies and MMAs in flight finish before a
+// CTA exits or frees TMEM always use this one.
+constexpr long long kWaitLimit = 1ll << 24;
+
+// Host side: the limit pipeline waits of the next launches get, and its
+// setter (rounds <= 0 restores kWaitLimit).
+long long wait_limit();
+void set_wait_limit(long long rounds);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -51,8 +60,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 // Bounded wait; returns false (and records `code`) when the limit runs out
 // or another role of the CTA has raised *abort.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code,
-                                          const int* abort = nullptr) {
-  for (long long i = 0; i < kWaitLimit; ++i) {
+                                          const int* abort = nullptr, long long limit = kWaitLimit) {
+  for (long long i = 0; i < limit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
     if (abort && (i & 1023) == 1023 && *(volatile const int*)abort) return false;
   }
@@ -77,6 +86,17 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+
+// D (FP32, TMEM) += A * B over K = 8 TF32 values (32 bytes) per row, A and
+// B K-major in shared memory (FP32 containers; the low 13 mantissa bits
+// must be zero, i.e. the values already rounded to TF32).
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
 }
 
@@ -109,6 +129,10 @@ __device__ __forceinline__ void tmem_wait_ld() {
 // be 128).  Returns false when the driver's encoder is unavailable or
 // rejects the map.
 bool make_map_bf16(CUtensorMap* m, const void* base, int rows, int K, int box_k, int box_rows);
+// The same over a row-major FP32 matrix [rows][cols] with a row pitch of
+// `pitch` elements (a multiple of 4), box box_k x box_rows, box_k * 4 = 128.
+bool make_map_f32(CUtensorMap* m, const void* base, int64_t rows, int cols, int64_t pitch, int box_k,
+                  int box_rows);
 
 }  // namespace tc
 }  // namespace rte

@@ -201,7 +201,7 @@ def test_learned_entry_gains_over_the_kdtree_entry(lib, cuda):
     import rt_entry_gb300 as r
     from rt_entry_gb300 import datasets as ds
     mix = ds.mixture_config(2)
-    base = mix.sample(100_000, ds.SEED_BASE)
+    base = mix.sample(400_000, ds.SEED_BASE)
     q = mix.sample(2000, ds.SEED_QUERY)
     train = mix.sample(262_144, ds.SEED_TRAIN)
     graph = ds.knn_graph(base, 64)
@@ -231,3 +231,44 @@ def test_learned_entry_gains_over_the_kdtree_entry(lib, cuda):
     print("untrained", g0)
     assert g0["rec_l"] - g0["rec_kd"] < 0.03, g0
     assert g0["rec_model_leaf"] < g["rec_model_leaf"] - 0.2, (g0, g)
+
+
+def test_bounded_waits_run_out_and_the_device_stays_usable(lib, cuda):
+    """Every pipeline wait of the tensor-core kernels is bounded.  With the
+    limit lowered to one try_wait round the waits run out at once: the GEMM
+    and the fused head return RTE_ETIMEOUT (their kernels let the copies and
+    MMAs in flight finish, free their tensor memory and exit), and with the
+    default restored the same calls in the same process give the right
+    results again."""
+    import torch
+
+    import rt_entry_gb300 as r
+    rng = np.random.default_rng(9)
+    a = r.bf16_bits(rng.standard_normal((1024, 256)).astype(np.float32))
+    b = r.bf16_bits(rng.standard_normal((512, 256)).astype(np.float32))
+    want = r.gemm_bf16(a, b)
+    M, dp, H, N = 512, 128, 128, 1024
+
+    def dev_bf16(shape):
+        return torch.from_numpy(r.bf16_bits(rng.standard_normal(shape).astype(np.float32) * 0.1)
+                                .view(np.int16)).cuda()
+
+    x, w1, w2, w3 = dev_bf16((M, dp)), dev_bf16((H, dp)), dev_bf16((H, H)), dev_bf16((N, H))
+    b1, b2, b3 = (torch.zeros(n, dtype=torch.float32, device="cuda") for n in (H, H, N))
+    cols_want = r.mlp_head_argmax(x, w1, b1, w2, b2, w3, b3)
+    torch.cuda.synchronize()
+    lib.rte_set_wait_limit(1)
+    try:
+        with pytest.raises(r.RteError) as e:
+            r.gemm_bf16(a, b)
+        assert e.value.status == r.RTE_ETIMEOUT, e.value
+        with pytest.raises(r.RteError) as e:
+            r.mlp_head_argmax(x, w1, b1, w2, b2, w3, b3)
+            torch.cuda.synchronize()
+        assert e.value.status == r.RTE_ETIMEOUT, e.value
+    finally:
+        lib.rte_set_wait_limit(0)
+    torch.cuda.synchronize()
+    assert np.array_equal(r.gemm_bf16(a, b), want)
+    cols = r.mlp_head_argmax(x, w1, b1, w2, b2, w3, b3)
+    assert torch.equal(cols, cols_want)

@@ -79,6 +79,23 @@ SWEEP = [
     (64, True, 32, 16, 1, 32, 4, 1, 5),
     (960, False, 64, 64, 1, 512, 3, 1, 100),    # 960 dims: 30 chunks of 32 per row
     (960, False, 32, 16, 2, 1024, 3, 0, 60),
+    # kernels built for any chunk count: dimensions without a specialised
+    # kernel (remainders of 1, 2 and 3 chunks past the 4-chunk slabs), and a
+    # specialised count whose (beam, batch) pair was not built (960, width 1
+    # over degree 32)
+    (160, True, 32, 64, 1, 512, 3, 1, 100),
+    (256, False, 64, 32, 1, 512, 3, 1, 100),
+    (416, True, 32, 128, 2, 1024, 3, 1, 100),
+    (736, False, 64, 16, 1, 512, 3, 0, 100),
+    (1000, False, 32, 64, 1, 512, 3, 1, 60),
+    (960, True, 32, 32, 1, 512, 3, 1, 100),
+    # degree-16 graphs: a 16-slot batch (width 1), two lists per batch
+    # register (width 2 and 4), with 16- to 64-slot pools
+    (128, True, 16, 64, 1, 512, 3, 1, 100),
+    (128, False, 16, 16, 1, 512, 3, 1, 100),
+    (64, True, 16, 32, 2, 1024, 3, 1, 100),
+    (96, False, 16, 128, 4, 2048, 3, 0, 100),
+    (320, False, 16, 32, 1, 512, 3, 1, 100),
 ]
 
 
@@ -148,6 +165,39 @@ def test_pca_against_fp64_and_reference_golden(lib, cuda):
     qp = idx.project(q)
     exact = (q.astype(np.float64) - z["mean"]) @ rot.astype(np.float64)
     assert np.abs(qp - exact).max() <= 1e-5 * np.abs(exact).max()
+
+
+@pytest.mark.parametrize("d,keep,nq", [(128, 128, 10000), (960, 960, 300), (100, 100, 777),
+                                        (96, 3, 500), (128, 48, 1000)])
+def test_tensor_core_projection_matches_fp64(lib, cuda, d, keep, nq):
+    """The projection (x - mean) V on the tensor cores (TF32, three-term
+    split, FP32 accumulation): queries and the projected base within 1e-5 of
+    the largest coordinate of an FP64 product of the same FP32 mean and
+    rotation, for one to four column blocks and K not a multiple of 32.  A
+    misaligned query buffer takes the FP32 FMA kernel, which must agree to
+    the same tolerance."""
+    import torch
+
+    import rt_entry_gb300 as r
+    rng = np.random.default_rng(d + keep)
+    base = (rng.standard_normal((2000, d)) * 3.0 + rng.uniform(0, 50, d)).astype(np.float32)
+    q = (rng.standard_normal((nq, d)) * 3.0 + rng.uniform(0, 50, d)).astype(np.float32)
+    idx = r.Index.from_arrays(base, np.zeros((2000, 32), np.int32)).build_pca(keep)
+    mean, rot, _ = idx.pca()
+    V = rot.astype(np.float64)[:, :keep]
+    exact = (q.astype(np.float64) - mean.astype(np.float64)) @ V
+    tol = 1e-5 * np.abs(exact).max()
+    qd = torch.from_numpy(q).cuda()
+    qp = idx.project(qd).cpu().numpy()
+    assert np.abs(qp - exact).max() <= tol
+    flat = torch.empty(nq * d + 1, dtype=torch.float32, device="cuda")
+    qm = flat[1:].view(nq, d)  # 4 bytes off the 16-byte alignment TMA needs
+    qm.copy_(qd)
+    qp_fma = idx.project(qm).cpu().numpy()
+    assert np.abs(qp_fma - exact).max() <= tol
+    pb = idx.search_base()
+    pexact = (base.astype(np.float64) - mean.astype(np.float64)) @ V
+    assert np.abs(pb - pexact).max() <= 1e-5 * np.abs(pexact).max()
 
 
 def test_pca_keep_dims_and_kdtree_consistency(lib, orc, cuda):
@@ -240,6 +290,27 @@ def test_low_precision_paths_match_oracle(lib, orc, cuda, prec, rerank, L):
     assert np.array_equal(dd, od)
 
 
+@pytest.mark.parametrize("L,W", [(16, 1), (64, 1), (32, 4)])
+@pytest.mark.parametrize("prec", [1, 2])
+def test_low_precision_paths_on_degree16_graph_match_oracle(lib, orc, cuda, prec, L, W):
+    """The BF16 tensor-core and FP8 paths over a degree-16 graph (a 16-slot
+    batch at width 1, four lists in two batch registers at width 4), with
+    the FP32 rerank: bit-exact against the oracle on the dequantised base
+    (integer-valued data keeps every BF16 term exact)."""
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(3000, 200, 128, True, seed=161 + prec + L)
+    graph = ds.knn_graph(base, 16)
+    idx = _index(base, graph, 32, 0.2)
+    _, _, pids = idx.kdtree()
+    hits = idx.locate(q)
+    low = idx.search_base_lowp(prec)
+    ids, dd = idx.search_projected(q, beam=L, k=L, search_width=W, precision=prec, rerank=1)
+    oids, od = orc.search(low, q, graph, L=L, k=L, search_width=W, leaf_pids=pids, hits=hits,
+                          rerank_base=base)
+    assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
+    assert np.array_equal(dd, od)
+
+
 @pytest.mark.parametrize("d", [128, 96])
 def test_bf16_tensor_core_distances_on_real_valued_data(lib, orc, cuda, d):
     """Real-valued data: the BF16 distance is |p|^2 + |q|^2 - 2 p.q with the
@@ -276,13 +347,15 @@ def test_bf16_tensor_core_distances_on_real_valued_data(lib, orc, cuda, d):
     assert rec_b >= rec_f - 0.01, (rec_b, rec_f)
 
 
+@pytest.mark.parametrize("d", [960, 200, 288])
 @pytest.mark.parametrize("prec", [1, 2])
-def test_high_dim_precisions_match_oracle(lib, orc, cuda, prec):
-    """960 dims (30 chunks): the BF16 and FP8 paths run the scalar distance
-    code there, so both are bit-exact against the oracle on the dequantised
+def test_high_dim_precisions_match_oracle(lib, orc, cuda, prec, d):
+    """Above 128 dims the BF16 and FP8 paths run the scalar distance code
+    (960: the 30-chunk kernel; 200 and 288: the kernels built for any chunk
+    count), so both are bit-exact against the oracle on the dequantised
     base, before and after the FP32 rerank, on real-valued data."""
     from rt_entry_gb300 import datasets as ds
-    base, q = _mixture(2500, 120, 960, False, seed=960 + prec)
+    base, q = _mixture(2500, 120, d, False, seed=d + prec)
     graph = ds.knn_graph(base, 64)
     idx = _index(base, graph, 32, 0.2)
     _, _, pids = idx.kdtree()
@@ -364,6 +437,11 @@ def test_parameter_errors(lib, cuda):
         with pytest.raises(r.RteError) as e:
             idx.search_projected(q, **kw)
         assert e.value.status == r.RTE_EINVAL, kw
+    # graphs below degree 16 have no kernel (a list must fill half a warp)
+    idx8 = r.Index.from_arrays(base, ds.knn_graph(base, 8)).build_kdtree(32, 0.2)
+    with pytest.raises(r.RteError) as e:
+        idx8.search_projected(q, beam=64, k=10)
+    assert e.value.status == r.RTE_EINVAL and "degree" in str(e.value)
     # empty batch is fine
     ids, dd = idx.search_projected(q[:0], beam=64, k=10)
     assert ids.shape == (0, 10)
@@ -386,3 +464,58 @@ def test_save_load_roundtrip(lib, cuda, tmp_path):
     idx2 = r.Index.load_dir(str(tmp_path / "ix"))
     ids2, dd2 = idx2.search(q, beam=64, k=10)
     assert np.array_equal(ids, ids2) and np.array_equal(dd, dd2)
+
+
+def test_load_reference_data_directory(lib, orc, cuda, tmp_path):
+    """An index opened from a data directory the reference's own code wrote
+    (mean.fbin and O.fbin by PCA::save_mean_rotation, pca_base.fbin by
+    PCA::save_result, 32_0.aabbs from its Kdtree): the search space is
+    pca_base.fbin as stored, the kd-tree equals the file's leaves, and the
+    search is bit-exact against the oracle on those inputs.  The same holds
+    for a directory this library saved, which reopens into an index with
+    identical results.  A leaf file of another base is rejected."""
+    import rt_entry_gb300 as r
+    sys.path.insert(0, GOLD)
+    import make_refdir_golden as refdir
+    d = str(tmp_path / "ref")
+    os.mkdir(d)
+    q, leaf = refdir.materialise(d)
+    idx = r.Index.load_reference(d, os.path.join(d, "base.bvecs"), os.path.join(d, "graph.int32"),
+                                 leaf_size=leaf, expand_ratio=0.2)
+    info = idx.info
+    assert info.has_pca and info.has_kdtree and info.degree == refdir.R
+    pb = r.read_vectors(os.path.join(d, "pca_base.fbin"))
+    assert np.array_equal(idx.search_base(), pb)
+    tight, expanded, pids = idx.kdtree()
+    raw = open(os.path.join(d, f"{leaf}_0.aabbs"), "rb").read()
+    nl = int(np.frombuffer(raw[:4], np.int32)[0])
+    assert nl == info.n_leaves
+    assert np.array_equal(tight, np.frombuffer(raw[8:8 + 24 * nl], np.float32).reshape(nl, 6))
+    assert np.array_equal(pids, np.frombuffer(raw[8 + 24 * nl:], np.int32).reshape(nl, leaf))
+    mean = r.read_vectors(os.path.join(d, "mean.fbin"))[0].astype(np.float64)
+    O = r.read_vectors(os.path.join(d, "O.fbin")).astype(np.float64)
+    qp = idx.project(q)
+    exact = (q.astype(np.float64) - mean) @ O
+    assert np.abs(qp - exact).max() <= 1e-5 * np.abs(exact).max()
+    graph = np.fromfile(os.path.join(d, "graph.int32"), np.int32).reshape(-1, refdir.R)
+    ids, dd = idx.search(q, beam=64, k=64)
+    oids, od = orc.search(pb, qp, graph, L=64, k=64, leaf_pids=pids, hits=orc.locate(expanded, qp))
+    assert np.array_equal(ids, oids) and np.array_equal(dd, od)
+    # a directory this library saved (the same layouts) reopens identically
+    own = r.Index.from_arrays(r.read_vectors(os.path.join(d, "base.fvecs")), graph).build_pca()
+    own.build_kdtree(leaf, 0.2)
+    s = str(tmp_path / "own")
+    own.save(s)
+    again = r.Index.load_reference(s, os.path.join(s, "base.fbin"), os.path.join(s, "graph.ibin"),
+                                   leaf_size=leaf, expand_ratio=0.2)
+    ids1, dd1 = own.search(q, beam=64, k=10)
+    ids2, dd2 = again.search(q, beam=64, k=10)
+    assert np.array_equal(ids1, ids2) and np.array_equal(dd1, dd2)
+    # the leaves of another base: rejected
+    import shutil
+    shutil.copy(os.path.join(d, f"{leaf}_0.aabbs"), os.path.join(s, f"{leaf}_0.aabbs"))
+    os.remove(os.path.join(s, "pca_base.fbin"))
+    with pytest.raises(r.RteError) as e:
+        r.Index.load_reference(s, os.path.join(s, "base.fbin"), os.path.join(s, "graph.ibin"),
+                               leaf_size=leaf, expand_ratio=0.2)
+    assert e.value.status == r.RTE_EIO and "aabbs" in str(e.value)
