@@ -715,7 +715,9 @@ def main():
         total_s = max_over_ranks(sum(head_ms) / 1000.0, device=dev)  # the slowest replica
         value = nq * args.steps * world / total_s
         head_recall = ds.recall_at(head_ids, w.gt, K_TOP)
+        torch.cuda.nvtx.range_push("rte_timed_plain")
         plain_ms = B.time_path(idx, qd, p_plain, args.steps, args.warmup, out_ids, out_d)
+        torch.cuda.nvtx.range_pop()
         plain_ids = out_ids.cpu().numpy()
         plain_qps = nq * len(plain_ms) / (sum(plain_ms) / 1000.0)
         plain_recall = ds.recall_at(plain_ids, w.gt, K_TOP)

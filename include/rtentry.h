@@ -152,6 +152,8 @@ rte_status rte_search_projected(rte_index* idx, const float* projected, const in
  * a framework whose allocator owns the device.  Differences from
  * rte_search_projected:
  *   - every pointer must be device memory; entry_mode random or kd-tree;
+ *   - a BF16 or FP8 search needs that copy to exist already
+ *     (rte_index_prepare, or an earlier search): RTE_ESTATE otherwise;
  *   - at most RTE_NOALLOC_MAX_QUERIES queries per call (RTE_EINVAL beyond);
  *   - its scratch (each query's leaf and the search's work counter, about
  *     256 KB) is one fixed array inside the library that every GPU holds
@@ -263,6 +265,22 @@ rte_status rte_read_vectors(const char* path, float* out, int64_t capacity, int6
  * <leaf_size>_0.aabbs in the reference's layouts, entry.cu:171-190). */
 rte_status rte_index_save(const rte_index* idx, const char* dir);
 rte_status rte_index_load_dir(const char* dir, int device, rte_index** out);
+
+/* Device copies an index can hold besides its FP32 search space.  An index
+ * starts with the FP32 search space and the raw base (the vectors as given:
+ * PCA builds, rerank 2 and rte_index_save read them).  The BF16 and FP8
+ * copies (precision 1 and 2) are made from the FP32 copy on the first
+ * search that needs them, or now by rte_index_prepare -- before a stream
+ * capture or rte_search_projected_noalloc, which cannot make them.
+ * rte_index_release frees copies once no search on the index is in flight;
+ * the BF16 and FP8 copies come back on their next use, the raw base does
+ * not (the calls that need it then return RTE_ESTATE).  No counterpart in
+ * the reference, which keeps one FP32 copy. */
+#define RTE_COPY_BF16 1u
+#define RTE_COPY_FP8 2u
+#define RTE_COPY_RAW 4u
+rte_status rte_index_prepare(rte_index* idx, unsigned copies);
+rte_status rte_index_release(rte_index* idx, unsigned copies);
 
 void rte_index_free(rte_index* idx);
 

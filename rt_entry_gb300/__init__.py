@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(_HERE, "_build", "librtentry.so")
 
 RTE_OK, RTE_EINVAL, RTE_ENOMEM, RTE_EIO, RTE_ECUDA, RTE_ETIMEOUT, RTE_ESTATE = range(7)
 PREC_FP32, PREC_BF16, PREC_FP8 = 0, 1, 2
+COPY_BF16, COPY_FP8, COPY_RAW = 1, 2, 4
 ENTRY_RANDOM, ENTRY_KDTREE, ENTRY_LEARNED = 0, 1, 2
 MAX_DIST = np.float32(536870912.0)
 
@@ -33,7 +34,7 @@ EXPORTS = (
     "rte_default_train_params", "rte_learned_train", "rte_learned_predict", "rte_mlp_grad_check",
     "rte_search_projected_noalloc", "rte_gemm_bf16_bias_argmax", "rte_mlp_head_argmax", "rte_knn_graph", "rte_locate_multi", "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
     "rte_batcher_free", "rte_autotune", "rte_set_wait_limit", "rte_index_load_reference",
-    "rte_read_vectors",
+    "rte_read_vectors", "rte_index_prepare", "rte_index_release",
 )
 
 
@@ -142,6 +143,8 @@ def load_library(path: str = LIB_PATH):
         "rte_index_load_reference": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, i32, i32,
                                       ctypes.c_float, i32, PP], i32),
         "rte_read_vectors": ([ctypes.c_char_p, P, i64, ctypes.POINTER(i64), ctypes.POINTER(i32)], i32),
+        "rte_index_prepare": ([P, ctypes.c_uint], i32),
+        "rte_index_release": ([P, ctypes.c_uint], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -389,6 +392,16 @@ class Index:
 
     def __exit__(self, *a):
         self.close()
+
+    def prepare(self, copies: int):
+        """Make the BF16 (COPY_BF16) / FP8 (COPY_FP8) copies now."""
+        _check(load_library().rte_index_prepare(self._h, copies))
+        return self
+
+    def release(self, copies: int):
+        """Free the BF16 / FP8 copies (made again on next use) or the raw base."""
+        _check(load_library().rte_index_release(self._h, copies))
+        return self
 
     # ---- build steps ----------------------------------------------------
     def build_pca(self, keep_dims: int = 0):

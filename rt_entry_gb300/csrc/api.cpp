@@ -36,6 +36,35 @@ rte_status fail(rte_status s, const std::string& msg) {
   return s;
 }
 void clear_error() { g_err.clear(); }
+
+rte_status ensure_precision(rte_index* x, int precision) {
+  if (precision != RTE_PREC_BF16 && precision != RTE_PREC_FP8) return RTE_OK;
+  std::lock_guard<std::mutex> lk(x->copy_mu);
+  if (precision == RTE_PREC_BF16 ? x->il16.p != nullptr : x->il8.p != nullptr) return RTE_OK;
+  DeviceGuard g(x->device);
+  const size_t n = 32 * (size_t)x->C * x->np;
+  if (precision == RTE_PREC_BF16) {
+    DevBuf<uint16_t> il16;
+    DevBuf<float> norm16;
+    RTE_CUDA(il16.alloc(n));
+    RTE_CUDA(norm16.alloc(x->np));
+    RTE_CUDA(launch_lowp_copies(x->il32.p, x->np, x->C, il16.p, nullptr, nullptr, 0));
+    RTE_CUDA(launch_bf16_norms(il16.p, x->np, x->C, norm16.p, 0));
+    RTE_CUDA(cudaStreamSynchronize(0));
+    x->il16 = std::move(il16);
+    x->norm16 = std::move(norm16);
+  } else {
+    DevBuf<uint8_t> il8;
+    DevBuf<float> scale8;
+    RTE_CUDA(il8.alloc(n));
+    RTE_CUDA(scale8.alloc(x->np));
+    RTE_CUDA(launch_lowp_copies(x->il32.p, x->np, x->C, nullptr, il8.p, scale8.p, 0));
+    RTE_CUDA(cudaStreamSynchronize(0));
+    x->il8 = std::move(il8);
+    x->scale8 = std::move(scale8);
+  }
+  return RTE_OK;
+}
 // Host or device memory?  Unregistered host memory reports
 // cudaMemoryTypeUnregistered; pinned host memory cudaMemoryTypeHost.
 bool is_device_ptr(const void* p) {
@@ -63,22 +92,25 @@ size_t index_bytes(const rte_index* x) {
          x->d_nodes.bytes() + x->d_wide.bytes() + x->d_pids.bytes();
 }
 
-// (Re)build the lane-interleaved FP32/BF16/FP8 copies of the search space
-// from a row-major device array [np][search_dim].
+// (Re)build the lane-interleaved FP32 copy of the search space from a
+// row-major device array [np][search_dim]; the BF16 and FP8 copies of the
+// previous search space are dropped (they are made again on first use).
 rte_status make_search_space(rte_index* x, const float* rm) {
   x->C = chunks_of(x->search_dim);
   const size_t row = 32 * (size_t)x->C;
+  {
+    std::lock_guard<std::mutex> lk(x->copy_mu);
+    x->il16.reset();
+    x->norm16.reset();
+    x->il8.reset();
+    x->scale8.reset();
+  }
   RTE_CUDA(x->il32.alloc(row * x->np));
-  RTE_CUDA(x->il16.alloc(row * x->np));
-  RTE_CUDA(x->il8.alloc(row * x->np));
-  RTE_CUDA(x->scale8.alloc(x->np));
-  RTE_CUDA(x->norm16.alloc(x->np));
   DevBuf<float> xyz;
   RTE_CUDA(xyz.alloc(3 * x->np));
   if (x->search_dim < 3) RTE_CUDA(cudaMemset(xyz.p, 0, xyz.bytes()));
-  RTE_CUDA(launch_interleave(rm, x->np, x->search_dim, x->C, x->il32.p, x->il16.p, x->il8.p,
-                             x->scale8.p, xyz.p, 0));
-  RTE_CUDA(launch_bf16_norms(x->il16.p, x->np, x->C, x->norm16.p, 0));
+  RTE_CUDA(launch_interleave(rm, x->np, x->search_dim, x->C, x->il32.p, nullptr, nullptr, nullptr, xyz.p,
+                             0));
   x->xyz.resize(3 * x->np);
   RTE_CUDA(cudaMemcpy(x->xyz.data(), xyz.p, xyz.bytes(), cudaMemcpyDeviceToHost));
   RTE_CUDA(cudaDeviceSynchronize());
@@ -266,6 +298,9 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   const bool full_rerank = prm->rerank == 2;
   if (full_rerank && already_projected)
     return fail(RTE_EINVAL, "rerank 2 needs the original queries: use rte_search");
+  if (full_rerank && !x->raw.p) return fail(RTE_ESTATE, "rerank 2 needs the raw base, which was released");
+  s = ensure_precision(x, prm->precision);
+  if (s != RTE_OK) return s;
   const float* qp = d_queries;
   AsyncBuf proj, hitsb, work, xb, zs;
   // learned entries without caller hits: the projection also writes the
@@ -472,6 +507,39 @@ rte_status rte_index_load(const char* base_path, const char* graph_path, int dev
   return create_index(base.data(), np, dim, graph.data(), degree, device, out);
 }
 
+rte_status rte_index_prepare(rte_index* x, unsigned copies) {
+  g_err.clear();
+  if (!x) return fail(RTE_EINVAL, "index is NULL");
+  if (copies & ~(unsigned)(RTE_COPY_BF16 | RTE_COPY_FP8 | RTE_COPY_RAW))
+    return fail(RTE_EINVAL, "unknown copy flags");
+  if ((copies & RTE_COPY_RAW) && !x->raw.p)
+    return fail(RTE_ESTATE, "the raw base was released and cannot be made again");
+  rte_status s = RTE_OK;
+  if (copies & RTE_COPY_BF16) s = ensure_precision(x, RTE_PREC_BF16);
+  if (s == RTE_OK && (copies & RTE_COPY_FP8)) s = ensure_precision(x, RTE_PREC_FP8);
+  return s;
+}
+
+rte_status rte_index_release(rte_index* x, unsigned copies) {
+  g_err.clear();
+  if (!x) return fail(RTE_EINVAL, "index is NULL");
+  if (copies & ~(unsigned)(RTE_COPY_BF16 | RTE_COPY_FP8 | RTE_COPY_RAW))
+    return fail(RTE_EINVAL, "unknown copy flags");
+  DeviceGuard g(x->device);
+  RTE_CUDA(cudaDeviceSynchronize());  // no search may still read what is freed
+  std::lock_guard<std::mutex> lk(x->copy_mu);
+  if (copies & RTE_COPY_BF16) {
+    x->il16.reset();
+    x->norm16.reset();
+  }
+  if (copies & RTE_COPY_FP8) {
+    x->il8.reset();
+    x->scale8.reset();
+  }
+  if (copies & RTE_COPY_RAW) x->raw.reset();
+  return RTE_OK;
+}
+
 void rte_index_free(rte_index* idx) {
   if (!idx) return;
   DeviceGuard g(idx->device);
@@ -488,6 +556,7 @@ rte_status install_pca(rte_index* x, const float* mean, const float* rotation, i
                        const float* projected, int ld) {
   if (keep_dims == 0) keep_dims = x->dim;
   if (keep_dims < 3 || keep_dims > x->dim) return fail(RTE_EINVAL, "keep_dims must be in [3, dim]");
+  if (!projected && !x->raw.p) return fail(RTE_ESTATE, "the raw base was released (rte_index_release)");
   DeviceGuard g(x->device);
   const int d = x->dim;
   x->mean32.assign(mean, mean + d);
@@ -616,6 +685,7 @@ rte_status rte_read_vectors(const char* path, float* out, int64_t capacity, int6
 rte_status rte_build_pca(rte_index* x, int keep_dims) {
   g_err.clear();
   if (!x) return fail(RTE_EINVAL, "index is NULL");
+  if (!x->raw.p) return fail(RTE_ESTATE, "the raw base was released (rte_index_release)");
   if (x->np < 2) return fail(RTE_EINVAL, "PCA needs at least two vectors");
   DeviceGuard g(x->device);
   const int d = x->dim;
@@ -921,6 +991,8 @@ rte_status rte_get_search_base_lowp(const rte_index* x, int precision, float* ou
   if (!x || !out) return fail(RTE_EINVAL, "NULL argument");
   if (precision != RTE_PREC_BF16 && precision != RTE_PREC_FP8)
     return fail(RTE_EINVAL, "precision must be RTE_PREC_BF16 or RTE_PREC_FP8");
+  rte_status s = ensure_precision(const_cast<rte_index*>(x), precision);
+  if (s != RTE_OK) return s;
   DeviceGuard g(x->device);
   DevBuf<float> tmp;
   RTE_CUDA(tmp.alloc((size_t)x->np * x->search_dim));
@@ -943,6 +1015,7 @@ rte_status rte_get_kdtree(const rte_index* x, float* tight, float* expanded, int
 rte_status rte_index_save(const rte_index* x, const char* dir) {
   g_err.clear();
   if (!x || !dir) return fail(RTE_EINVAL, "NULL argument");
+  if (!x->raw.p) return fail(RTE_ESTATE, "the raw base was released (rte_index_release)");
   DeviceGuard g(x->device);
   std::string err;
   std::vector<float> raw((size_t)x->np * x->dim);

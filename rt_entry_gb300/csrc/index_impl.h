@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -13,6 +14,9 @@
 namespace rte {
 
 rte_status fail(rte_status s, const std::string& msg);
+// The BF16 (precision 1) or FP8 (2) copy of the search space, made now if
+// the index has none; precision 0 needs nothing.  Synchronous.
+rte_status ensure_precision(rte_index* x, int precision);
 void clear_error();
 bool is_device_ptr(const void* p);
 
@@ -132,10 +136,13 @@ struct rte_index {
   // search space
   int C = 0;
   rte::DevBuf<float> il32;
+  // reduced-precision copies, made from il32 on first use or by
+  // rte_index_prepare (under copy_mu), freed by rte_index_release
   rte::DevBuf<uint16_t> il16;
   rte::DevBuf<uint8_t> il8;
   rte::DevBuf<float> scale8;
   rte::DevBuf<float> norm16;  // squared norms of the BF16 rows
+  std::mutex copy_mu;
   std::vector<float> xyz;  // first three search-space coordinates [np][3]
   // kd-tree
   bool has_kdtree = false;

@@ -278,6 +278,36 @@ __global__ void interleave_rows(const float* __restrict__ src, int64_t n, int d,
   }
 }
 
+// The BF16 and FP8 copies from the interleaved FP32 copy, one warp per row:
+// the same offsets, roundings and per-row scale (max |x| / 448 over the
+// row's dims) as interleave_rows writes from row-major input.
+__global__ void lowp_from_il32(const float* __restrict__ il32, int64_t n, int C,
+                               __nv_bfloat16* __restrict__ il16, uint8_t* __restrict__ il8,
+                               float* __restrict__ scale8) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n; r += nwarps) {
+    const float* s = il32 + r * (32 * C);
+    float amax = 0.0f;
+    for (int c = 0; c < C; ++c) {
+      const int64_t o = interleaved_offset(c, lane, C);
+      const float v = s[o];
+      amax = fmaxf(amax, fabsf(v));
+      if (il16) il16[r * (32 * C) + o] = __float2bfloat16_rn(v);
+    }
+    if (il8) {
+      for (int off = 16; off >= 1; off >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, off));
+      const float sc = amax > 0.0f ? amax / 448.0f : 1.0f;
+      if (lane == 0) scale8[r] = sc;
+      for (int c = 0; c < C; ++c) {
+        const int64_t o = interleaved_offset(c, lane, C);
+        il8[r * (32 * C) + o] = (uint8_t)__nv_cvt_float_to_fp8(__fdiv_rn(s[o], sc), __NV_SATFINITE, __NV_E4M3);
+      }
+    }
+  }
+}
+
 __global__ void deinterleave_rows(const float* __restrict__ il32, int64_t n, int d, int C,
                                   float* __restrict__ dst) {
   const int lane = threadIdx.x & 31;
@@ -635,6 +665,14 @@ cudaError_t launch_project_bf16_dyn(const float* x, int64_t cap, const int* n_de
   project_rows<true><<<grid, kPrThreads, 0, st>>>(x, cap, d, xstride, mean, V, vstride, k, out, ostride, n_dev,
                                                   reinterpret_cast<__nv_bfloat16*>(out16), s16, ld16, zero,
                                                   zero_words);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lowp_copies(const float* il32, int64_t n, int C, void* il16, uint8_t* il8,
+                               float* scale8, cudaStream_t st) {
+  const int64_t blocks = std::min<int64_t>((n + 7) / 8, 65535 * 8);
+  lowp_from_il32<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(
+      il32, n, C, reinterpret_cast<__nv_bfloat16*>(il16), il8, scale8);
   return cudaGetLastError();
 }
 

@@ -86,6 +86,11 @@ cudaError_t launch_interleave(const float* src, int64_t n, int d, int C, float* 
                               uint8_t* il8, float* scale8, float* xyz, cudaStream_t st);
 cudaError_t launch_deinterleave(const float* il32, int64_t n, int d, int C, float* dst,
                                 cudaStream_t st);
+// The BF16 copy (il16, may be null) and the FP8 copy with per-row scales
+// (il8 and scale8, may be null) made from the interleaved FP32 copy, equal
+// to what launch_interleave writes from row-major input.
+cudaError_t launch_lowp_copies(const float* il32, int64_t n, int C, void* il16, uint8_t* il8,
+                               float* scale8, cudaStream_t st);
 // Squared norm of every BF16 row (FP64 sum of the BF16 values squared,
 // rounded to FP32).
 cudaError_t launch_bf16_norms(const uint16_t* il16, int64_t n, int C, float* out, cudaStream_t st);

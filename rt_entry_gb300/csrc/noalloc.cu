@@ -99,6 +99,9 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   if (params->rerank == 2)
     return fail(RTE_EINVAL, "rerank 2 needs the original queries: use rte_search");
   if (params->max_hits > 1) return fail(RTE_EINVAL, "max_hits > 1 needs rte_search");
+  // making a reduced-precision copy would allocate
+  if ((params->precision == RTE_PREC_BF16 && !x->il16.p) || (params->precision == RTE_PREC_FP8 && !x->il8.p))
+    return fail(RTE_ESTATE, "the index has no copy in this precision: call rte_index_prepare first");
   if (nq == 0) return RTE_OK;
   if (!projected || !out_ids) return fail(RTE_EINVAL, "NULL argument");
   // inputs and outputs must already be device memory: copying host data

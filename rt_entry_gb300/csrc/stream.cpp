@@ -206,6 +206,9 @@ extern "C" rte_status rte_batcher_create(rte_index* x, int64_t max_nq,
   if (params->rerank == 2) return fail(RTE_EINVAL, "the batcher does not rerank against the original rows");
   if (params->max_hits > 1) return fail(RTE_EINVAL, "the batcher locates one leaf per query");
   DeviceGuard guard(x->device);
+  // the copy the search reads must exist before the graph is captured
+  rte_status ps = ensure_precision(x, params->precision);
+  if (ps != RTE_OK) return ps;
   auto* b = new rte_batcher();
   b->idx = x;
   b->prm = *params;

@@ -519,3 +519,42 @@ def test_load_reference_data_directory(lib, orc, cuda, tmp_path):
         r.Index.load_reference(s, os.path.join(s, "base.fbin"), os.path.join(s, "graph.ibin"),
                                leaf_size=leaf, expand_ratio=0.2)
     assert e.value.status == r.RTE_EIO and "aabbs" in str(e.value)
+
+
+def test_reduced_precision_copies_made_on_use_and_released(lib, cuda):
+    """An index holds only its FP32 search space and the raw base until a
+    BF16 or FP8 search needs more; copies made on first use, made ahead by
+    rte_index_prepare, or made again after rte_index_release all give the
+    same results.  Releasing the raw base turns the calls that read it into
+    RTE_ESTATE and leaves the search working."""
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(3000, 100, 128, True, seed=77)
+    graph = ds.knn_graph(base, 32)
+    idx = _index(base, graph)
+    i0 = idx.info
+    assert not i0.has_bf16 and not i0.has_fp8
+    ids32, d32 = idx.search_projected(q, beam=64, k=10)
+    assert idx.info.device_bytes == i0.device_bytes
+    ids16, d16 = idx.search_projected(q, beam=64, k=10, precision=r.PREC_BF16, rerank=1)
+    i1 = idx.info
+    assert i1.has_bf16 and not i1.has_fp8 and i1.device_bytes > i0.device_bytes
+    ahead = _index(base, graph).prepare(r.COPY_BF16 | r.COPY_FP8)
+    assert ahead.info.has_bf16 and ahead.info.has_fp8
+    got = ahead.search_projected(q, beam=64, k=10, precision=r.PREC_BF16, rerank=1)
+    assert np.array_equal(got[0], ids16) and np.array_equal(got[1], d16)
+    fp8 = ahead.search_projected(q, beam=64, k=10, precision=r.PREC_FP8, rerank=1)
+    mine = idx.search_projected(q, beam=64, k=10, precision=r.PREC_FP8, rerank=1)
+    assert np.array_equal(mine[0], fp8[0]) and np.array_equal(mine[1], fp8[1])
+    idx.release(r.COPY_BF16 | r.COPY_FP8)
+    assert not idx.info.has_bf16 and not idx.info.has_fp8
+    again = idx.search_projected(q, beam=64, k=10, precision=r.PREC_BF16, rerank=1)
+    assert np.array_equal(again[0], ids16) and np.array_equal(again[1], d16)
+    idx.release(r.COPY_RAW)
+    assert idx.info.device_bytes < i1.device_bytes
+    for call in (lambda: idx.build_pca(), lambda: idx.search(q, beam=64, k=10, rerank=2)):
+        with pytest.raises(r.RteError) as e:
+            call()
+        assert e.value.status == r.RTE_ESTATE
+    ids, dd = idx.search_projected(q, beam=64, k=10)
+    assert np.array_equal(ids, ids32) and np.array_equal(dd, d32)
