@@ -772,7 +772,7 @@ def main():
     clocks = clk.summary()
 
     # ---- CPU baseline: the oracle port of the plain search on the host cores ----
-    cpu = merge_idle = None
+    cpu = merge_idle = merge_few = None
     if rank == 0:
         import oracle
         pb = idx.search_base()
@@ -796,6 +796,10 @@ def main():
                                    n_threads=nthreads, with_counters=True)
         merge_idle = {f"plain_beam{Lp}": round(float(ocnt[:, 5].sum() / ocnt[:, 4].sum()), 4),
                       f"learned_beam{Lh}_fp32": round(float(lcnt[:, 5].sum() / lcnt[:, 4].sum()), 4)}
+        # main-loop batches the kernel merges by rank (1..8 distinct
+        # distances below the pool's largest), as a share of all merges
+        merge_few = {f"plain_beam{Lp}": round(float(ocnt[:, 6].sum() / ocnt[:, 4].sum()), 4),
+                     f"learned_beam{Lh}_fp32": round(float(lcnt[:, 6].sum() / lcnt[:, 4].sum()), 4)}
 
     stream_res = stream_kd = None
     if lead and not args.no_stream:
@@ -844,7 +848,7 @@ def main():
                "speedup_vs_plain": value / plain_qps,
                "roofline": roof_head,
                "roofline_plain": roof_plain,
-               "merge_idle_frac": merge_idle,
+               "merge_idle_frac": merge_idle, "merge_few_frac": merge_few,
                "reference_kernel_gb300": ref_kernel,
                "config2_precision": prec2,
                "config2_k100": k100,

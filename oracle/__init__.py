@@ -80,15 +80,16 @@ def build_reference() -> bool:
     return True
 
 
-N_COUNTERS = 6  # fields of Counters
+N_COUNTERS = 7  # fields of Counters
 
 
 class Counters(ctypes.Structure):
     """Per-query work counters (orc_counters): entries_valid, expanded,
-    dist_evals, iterations, merges, merges_idle."""
+    dist_evals, iterations, merges, merges_idle, merges_few."""
     _fields_ = [("entries_valid", ctypes.c_int64), ("expanded", ctypes.c_int64),
                 ("dist_evals", ctypes.c_int64), ("iterations", ctypes.c_int64),
-                ("merges", ctypes.c_int64), ("merges_idle", ctypes.c_int64)]
+                ("merges", ctypes.c_int64), ("merges_idle", ctypes.c_int64),
+                ("merges_few", ctypes.c_int64)]
 
 
 def lib():

@@ -36,6 +36,9 @@ typedef struct {
   int64_t merges_idle;     /* of those, batches with no distance below the
                               pool's largest: the merge leaves the pool as
                               it was                                        */
+  int64_t merges_few;      /* main-loop batches with 1..8 pairwise distinct
+                              distances below the pool's largest (no NaN):
+                              the ones a merge by rank can serve            */
 } orc_counters;
 
 /* Beam search over a fixed-degree graph, GraphSearchKernel semantics

@@ -177,17 +177,35 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
   std::vector<Pair> na(L + B, Pair{ORC_MAX_DIST, np});  // :473-477
   Pair* batch = na.data() + L;
   Bloom bloom(A.bloom_words, A.bloom_hashes);
-  orc_counters c = {0, 0, 0, 0, 0, 0};
+  orc_counters c = {0, 0, 0, 0, 0, 0, 0};
 
   auto dist_of = [&](int id) { return orc_l2_ref(A.base + (int64_t)id * A.d, q, A.d); };
   // counts a merge, and whether any batch distance is below the pool's
-  // largest (otherwise the merge cannot change the pool)
-  auto count_merge = [&]() {
+  // largest the merge cannot change the pool)
+  // (otherwise the merge cannot change the pool); for a main-loop batch,
+  // also whether 1..8 pairwise distinct distances (no NaN) lie below it
+  auto count_merge = [&](bool main_loop) {
     c.merges++;
     const float pmax = na[L - 1].d;
-    for (int i = 0; i < B; ++i)
-      if (batch[i].d < pmax) return;
-    c.merges_idle++;
+    float below[9];
+    int m = 0;
+    bool nan = false;
+    for (int i = 0; i < B; ++i) {
+      nan |= batch[i].d != batch[i].d;
+      if (batch[i].d < pmax) {
+        if (m < 9) below[m] = batch[i].d;
+        ++m;
+      }
+    }
+    if (m == 0) {
+      c.merges_idle++;
+      return;
+    }
+    if (!main_loop || nan || m > 8) return;
+    for (int i = 0; i < m; ++i)
+      for (int j = i + 1; j < m; ++j)
+        if (below[i] == below[j]) return;
+    c.merges_few++;
   };
 
   // ---- entry phase (:479-959) ----
@@ -240,7 +258,7 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
         batch[i].d = dist_of(batch[i].id);
         c.entries_valid++;
       }
-    count_merge();
+    count_merge(false);
     batch_sort_desc(batch, B);
     merge_pool(na.data(), L, B, false);
   }
@@ -319,7 +337,7 @@ void search_one(const SearchArgs& A, const float* q, int64_t qid, int32_t hit, i
       batch[i].d = dist_of(batch[i].id);
       c.dist_evals++;
     }
-    count_merge();
+    count_merge(true);
     batch_sort_desc(batch, B);
     merge_pool(na.data(), L, B, true);
     for (iteration = 0; iteration < nchunks; iteration++) {  // :1495-1516

@@ -5,7 +5,13 @@
 // runs on: row i lists the R nearest rows j != i by exact squared L2
 // distance (FP64), in (distance, id) order.
 //
-//   1. Each row x is split into BF16 x_hi = bf16(x) and x_lo = bf16(x - x_hi);
+//   0. The rows are centred on their column mean mu (FP64 sums in a fixed
+//      order, rounded to FP32): c = fl(x - mu).  Distances do not change
+//      under a shift, and the error bound of step 3 scales with the norms of
+//      what the GEMM multiplies, so centring tightens it by |x| / |c| (about
+//      5x for values in [0, 1] around 0.5).
+//   1. Each centred row c is split into BF16 c_hi = bf16(c) and
+//      c_lo = bf16(c - c_hi);
 //      A = [hi | hi | lo] and B = [hi | lo | hi] along K, so one tensor-core
 //      GEMM (gemm_tc.cu, K = 3*dp) gives hi.hi + hi.lo + lo.hi, the dot
 //      product to about 2^-16 relative.
@@ -15,12 +21,15 @@
 //   3. Exact FP64 distances of the K candidates, sorted by (distance, id),
 //      self excluded (rerank_rows).  The row is certified exact when its R-th
 //      distance is below the left-out bound minus the approximation's error
-//      bound; rows that fail are redone with 1024 candidates, and a row that
+//      bound; rows that fail are redone with 1024 candidates selected from
+//      the same block of dot products (still in memory), and a row that
 //      fails again is an error.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <vector>
 
@@ -36,9 +45,32 @@ constexpr int kSelT = 16;                         // candidates kept per thread
 constexpr int kSelPool = kSelThreads * kSelT;     // 4096 merged per row
 constexpr int kMaxCand = 1024;                    // the retry's candidate count
 
-// Row split and norms: one warp per row.
-__global__ void split_rows(const float* __restrict__ x, int64_t n, int d, int dp,
-                           __nv_bfloat16* __restrict__ a, __nv_bfloat16* __restrict__ b,
+constexpr int kMeanSlices = 256;  // row slices of the column mean's first pass
+
+// Column sums of row slice blockIdx.y in FP64 (rows in order), one thread
+// per column: part[slice][c].
+__global__ void col_sum_slices(const float* __restrict__ x, int64_t n, int d, double* __restrict__ part) {
+  const int s = blockIdx.y;
+  const int64_t r0 = n * s / kMeanSlices, r1 = n * (s + 1) / kMeanSlices;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < d; c += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int64_t r = r0; r < r1; ++r) acc += (double)__ldg(x + r * d + c);
+    part[(int64_t)s * d + c] = acc;
+  }
+}
+
+// mu[c] = (sum of the slices' sums in slice order) / n, rounded to FP32.
+__global__ void col_mean_finish(const double* __restrict__ part, int64_t n, int d, float* __restrict__ mu) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d) return;
+  double acc = 0.0;
+  for (int s = 0; s < kMeanSlices; ++s) acc += part[(int64_t)s * d + c];
+  mu[c] = (float)(acc / (double)n);
+}
+
+// Centring, split and norms of the centred rows: one warp per row.
+__global__ void split_rows(const float* __restrict__ x, const float* __restrict__ mu, int64_t n, int d,
+                           int dp, __nv_bfloat16* __restrict__ a, __nv_bfloat16* __restrict__ b,
                            float* __restrict__ nrm32, double* __restrict__ nrm64) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -47,7 +79,7 @@ __global__ void split_rows(const float* __restrict__ x, int64_t n, int d, int dp
   for (int64_t r = warp; r < n; r += nwarps) {
     double s = 0.0;
     for (int c = lane; c < dp; c += 32) {
-      const float v = c < d ? x[r * d + c] : 0.0f;
+      const float v = c < d ? __fsub_rn(x[r * d + c], mu[c]) : 0.0f;
       const __nv_bfloat16 hi = __float2bfloat16_rn(v);
       const __nv_bfloat16 lo = __float2bfloat16_rn(__fsub_rn(v, __bfloat162float(hi)));
       a[r * ld + c] = hi;           // A = [hi | hi | lo]
@@ -97,15 +129,17 @@ __device__ void block_sort(float* sd, int* si) {
 // One block per row: approximate distances from the dot products in
 // D[row][0..n), the K smallest by (distance, id), and the smallest
 // approximate distance any left-out column can have.
+// With `local`, block i serves row local[i] of the block of dot products.
 __global__ void __launch_bounds__(kSelThreads) select_rows(const float* __restrict__ D, int64_t ld,
                                                            int64_t r0, int64_t n,
                                                            const float* __restrict__ nrm32, int K,
+                                                           const int32_t* __restrict__ local,
                                                            int32_t* __restrict__ cand,
                                                            float* __restrict__ excl) {
   __shared__ float sd[kSelPool];
   __shared__ int si[kSelPool];
   __shared__ float sdrop[kSelThreads];
-  const int r = blockIdx.x;
+  const int r = local ? local[blockIdx.x] : (int)blockIdx.x;
   const float qn = nrm32[r0 + r];
   float kd[kSelT];
   int ki[kSelT];
@@ -141,11 +175,12 @@ __global__ void __launch_bounds__(kSelThreads) select_rows(const float* __restri
   }
   __syncthreads();
   block_sort(sd, si);
-  for (int k = threadIdx.x; k < K; k += kSelThreads) cand[(int64_t)r * K + k] = si[k] < n ? si[k] : -1;
+  const int64_t o = blockIdx.x;
+  for (int k = threadIdx.x; k < K; k += kSelThreads) cand[o * K + k] = si[k] < n ? si[k] : -1;
   if (threadIdx.x == 0) {
     float m = K < kSelPool ? sd[K] : INFINITY;
     for (int t = 0; t < kSelThreads; ++t) m = fminf(m, sdrop[t]);
-    excl[r] = m;
+    excl[o] = m;
   }
 }
 
@@ -202,10 +237,15 @@ __global__ void __launch_bounds__(256) rerank_rows(const float* __restrict__ x, 
       }
       __syncthreads();
     }
-  // |approximate - exact| <= err for every column (hi/lo split, FP32 sums)
+  // |approximate - exact| <= err for every column: the hi/lo split and the
+  // FP32 sums over the centred rows (norms qnorm, at most max_norm), plus
+  // the centring's rounding -- each fl(x - mu) is off by at most 2^-24 of
+  // |x - mu|, which moves a squared distance by at most about
+  // 2^-23 (qnorm + max_norm)^2; the last term doubles that for room
   const double qnorm = sqrt(nrm64[gi]);
   const double err = (ldexp(1.0, -14) + d * ldexp(1.0, -21)) * qnorm * max_norm +
-                     ldexp(1.0, -20) * (nrm64[gi] + max_norm * max_norm);
+                     ldexp(1.0, -20) * (nrm64[gi] + max_norm * max_norm) +
+                     ldexp(1.0, -22) * (qnorm + max_norm) * (qnorm + max_norm);
   if (threadIdx.x == 0) {
     const bool ok = si[R - 1] != INT32_MAX && sd[R - 1] < (double)excl[r] - err;
     if (!ok) atomicAdd(failed, 1);
@@ -246,7 +286,7 @@ extern "C" rte_status rte_knn_graph(const float* base, int64_t n, int d, int deg
   // rows per block: the FP32 dot-product block stays under 8 GB
   int64_t mb = std::max<int64_t>(128, std::min<int64_t>(8192, (int64_t)(8ll << 30) / (n * 4)));
   mb = std::min<int64_t>(mb, n);
-  Buf xd, A, B, n32, n64, D, cand, excl, rows, fl, outd;
+  Buf xd, A, B, n32, n64, D, cand, excl, rows, fl, outd, part, mu, loc;
   const bool base_dev = is_device_ptr(base), graph_dev = is_device_ptr(graph);
   const float* x = base;
   if (!base_dev) {
@@ -268,8 +308,14 @@ extern "C" rte_status rte_knn_graph(const float* base, int64_t n, int d, int deg
     RTE_CUDA(outd.alloc((size_t)n * degree * 4));
     g = outd.as<int32_t>();
   }
+  RTE_CUDA(part.alloc((size_t)kMeanSlices * d * 8));
+  RTE_CUDA(mu.alloc((size_t)d * 4));
+  RTE_CUDA(loc.alloc((size_t)mb * 4));
+  col_sum_slices<<<dim3((unsigned)((d + 127) / 128), kMeanSlices), 128, 0, st>>>(x, n, d, part.as<double>());
+  col_mean_finish<<<(unsigned)((d + 127) / 128), 128, 0, st>>>(part.as<double>(), n, d, mu.as<float>());
   split_rows<<<(unsigned)std::min<int64_t>((n + 7) / 8, 65535), 256, 0, st>>>(
-      x, n, d, dp, A.as<__nv_bfloat16>(), B.as<__nv_bfloat16>(), n32.as<float>(), n64.as<double>());
+      x, mu.as<float>(), n, d, dp, A.as<__nv_bfloat16>(), B.as<__nv_bfloat16>(), n32.as<float>(),
+      n64.as<double>());
   RTE_CUDA(cudaGetLastError());
   std::vector<double> hn(n);
   RTE_CUDA(cudaMemcpyAsync(hn.data(), n64.p, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
@@ -280,10 +326,11 @@ extern "C" rte_status rte_knn_graph(const float* base, int64_t n, int d, int deg
   RTE_CUDA(errb.alloc(4));
   int* err = errb.as<int>();
   RTE_CUDA(cudaMemsetAsync(err, 0, 4, st));
-  std::vector<int64_t> hrows(mb);
-  std::vector<int32_t> hfirst(mb);
-  std::vector<int64_t> retry;
+  std::vector<int64_t> hrows(mb), rrows;
+  std::vector<int32_t> hfirst(mb), rlocal;
   const int Kp = 1 << (int)std::ceil(std::log2((double)std::max(K, 2)));
+  const int K2 = (int)std::min<int64_t>(kMaxCand, n);
+  int64_t n_retried = 0;
   for (int64_t r0 = 0; r0 < n; r0 += mb) {
     const int64_t m = std::min(mb, n - r0);
     GemmArgs ga{};
@@ -297,7 +344,7 @@ extern "C" rte_status rte_knn_graph(const float* base, int64_t n, int d, int deg
     ga.ldc = (int)n;
     ga.err = err;
     RTE_CUDA(gemm_bf16_tn(ga, st));
-    select_rows<<<(unsigned)m, kSelThreads, 0, st>>>(D.as<float>(), n, r0, n, n32.as<float>(), K,
+    select_rows<<<(unsigned)m, kSelThreads, 0, st>>>(D.as<float>(), n, r0, n, n32.as<float>(), K, nullptr,
                                                        cand.as<int32_t>(), excl.as<float>());
     RTE_CUDA(cudaGetLastError());
     for (int64_t i = 0; i < m; ++i) hrows[i] = r0 + i;
@@ -311,48 +358,40 @@ extern "C" rte_status rte_knn_graph(const float* base, int64_t n, int d, int deg
     int nfail = 0;
     RTE_CUDA(cudaMemcpyAsync(&nfail, fl.p, 4, cudaMemcpyDeviceToHost, st));
     RTE_CUDA(cudaStreamSynchronize(st));
-    if (nfail) {  // collect the rows that were not certified (first entry -1)
-      RTE_CUDA(cudaMemcpy2DAsync(hfirst.data(), 4, g + r0 * degree, (size_t)degree * 4, 4, (size_t)m,
-                                 cudaMemcpyDeviceToHost, st));
-      RTE_CUDA(cudaStreamSynchronize(st));
-      for (int64_t i = 0; i < m; ++i)
-        if (hfirst[i] < 0) retry.push_back(r0 + i);
-    }
-  }
-  // retry: 1024 candidates per row from a fresh selection over the row's
-  // own dot products
-  for (size_t t0 = 0; t0 < retry.size(); t0 += (size_t)mb) {
-    const int64_t m = std::min<int64_t>(mb, (int64_t)(retry.size() - t0));
-    for (int64_t i = 0; i < m; ++i) {
-      const int64_t gi = retry[t0 + i];
-      GemmArgs ga{};
-      ga.A = A.as<__nv_bfloat16>() + gi * 3 * dp;
-      ga.B = B.p;
-      ga.M = 1;
-      ga.N = (int)n;
-      ga.K = 3 * dp;
-      ga.epilogue = kEpiStoreF32;
-      ga.C = D.as<float>() + i * n;
-      ga.ldc = (int)n;
-      ga.err = err;
-      RTE_CUDA(gemm_bf16_tn(ga, st));
-      select_rows<<<1, kSelThreads, 0, st>>>(D.as<float>() + i * n, n, gi, n, n32.as<float>(),
-                                             (int)std::min<int64_t>(kMaxCand, n),
-                                             cand.as<int32_t>() + i * kMaxCand, excl.as<float>() + i);
-      RTE_CUDA(cudaGetLastError());
-    }
-    RTE_CUDA(cudaMemcpyAsync(rows.p, retry.data() + t0, m * 8, cudaMemcpyHostToDevice, st));
+    if (!nfail) continue;
+    // rows not certified (first entry -1): K2 candidates from the same
+    // block of dot products, which the next block's GEMM has not yet
+    // overwritten (same stream)
+    RTE_CUDA(cudaMemcpy2DAsync(hfirst.data(), 4, g + r0 * degree, (size_t)degree * 4, 4, (size_t)m,
+                               cudaMemcpyDeviceToHost, st));
+    RTE_CUDA(cudaStreamSynchronize(st));
+    rrows.clear();
+    rlocal.clear();
+    for (int64_t i = 0; i < m; ++i)
+      if (hfirst[i] < 0) {
+        rrows.push_back(r0 + i);
+        rlocal.push_back((int32_t)i);
+      }
+    const int64_t mr = (int64_t)rrows.size();
+    n_retried += mr;
+    RTE_CUDA(cudaMemcpyAsync(loc.p, rlocal.data(), mr * 4, cudaMemcpyHostToDevice, st));
+    RTE_CUDA(cudaMemcpyAsync(rows.p, rrows.data(), mr * 8, cudaMemcpyHostToDevice, st));
+    select_rows<<<(unsigned)mr, kSelThreads, 0, st>>>(D.as<float>(), n, r0, n, n32.as<float>(), K2,
+                                                        loc.as<int32_t>(), cand.as<int32_t>(),
+                                                        excl.as<float>());
+    RTE_CUDA(cudaGetLastError());
     RTE_CUDA(cudaMemsetAsync(fl.p, 0, 4, st));
-    const int k2 = (int)std::min<int64_t>(kMaxCand, n);
-    rerank_rows<<<(unsigned)m, 256, (size_t)kMaxCand * 12, st>>>(
-        x, d, rows.as<int64_t>(), cand.as<int32_t>(), k2, kMaxCand, excl.as<float>(), n64.as<double>(),
+    rerank_rows<<<(unsigned)mr, 256, (size_t)kMaxCand * 12, st>>>(
+        x, d, rows.as<int64_t>(), cand.as<int32_t>(), K2, kMaxCand, excl.as<float>(), n64.as<double>(),
         max_norm, degree, g, fl.as<int>());
     RTE_CUDA(cudaGetLastError());
-    int nfail = 0;
     RTE_CUDA(cudaMemcpyAsync(&nfail, fl.p, 4, cudaMemcpyDeviceToHost, st));
     RTE_CUDA(cudaStreamSynchronize(st));
     if (nfail) return fail(RTE_EIO, "kNN graph: " + std::to_string(nfail) + " rows could not be certified exact");
   }
+  if (getenv("RTE_KNN_VERBOSE"))
+    fprintf(stderr, "rte_knn_graph: n %lld d %d degree %d: %lld rows retried with %d candidates\n",
+            (long long)n, d, degree, (long long)n_retried, K2);
   int herr = 0;
   RTE_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
   if (!graph_dev) RTE_CUDA(cudaMemcpyAsync(graph, g, (size_t)n * degree * 4, cudaMemcpyDeviceToHost, st));

@@ -182,6 +182,27 @@ __device__ __forceinline__ void sort_batch_desc(float (&d)[NB], int (&id)[NB], i
   }
 }
 
+// The pool's ascending half-cleaner (graph_search.cuh:933-957): compare-
+// exchanges at distances L/2 .. 1, in registers for distances >= 32.
+template <int NL>
+__device__ __forceinline__ void half_clean(float (&pd)[pool_regs(NL)], int (&pi)[pool_regs(NL)], int lane) {
+  constexpr int L = pool_slots(NL), PR = pool_regs(NL);
+#pragma unroll
+  for (int sub = L / 2; sub >= 1; sub >>= 1) {
+    if (sub >= 32) {
+      const int rs = sub >> 5;
+#pragma unroll
+      for (int j = 0; j < PR; ++j) {
+        if (j & rs) continue;
+        cx_regs(pd[j], pi[j], pd[j + rs], pi[j + rs], false);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < PR; ++j) cx_lanes(pd[j], pi[j], sub, false, lane);
+    }
+  }
+}
+
 // Pool/batch merge then the ascending half-cleaner (graph_search.cuh:921-957,
 // :1454-1493).  Pool slot L-n+i meets batch slot B-n+i (n = min(L,B)); both
 // are in the same lane.  The main loop skips a batch slot holding MAX.
@@ -206,21 +227,7 @@ __device__ __forceinline__ void merge_pool(float (&pd)[pool_regs(NL)], int (&pi)
       pd[PR - 1] = od;
       pi[PR - 1] = oi;
     }
-    constexpr int L = pool_slots(NL);
-#pragma unroll
-    for (int sub = L / 2; sub >= 1; sub >>= 1) {
-      if (sub >= 32) {
-        const int rs = sub >> 5;
-#pragma unroll
-        for (int j = 0; j < PR; ++j) {
-          if (j & rs) continue;
-          cx_regs(pd[j], pi[j], pd[j + rs], pi[j + rs], false);
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < PR; ++j) cx_lanes(pd[j], pi[j], sub, false, lane);
-      }
-    }
+    half_clean<NL>(pd, pi, lane);
   } else if constexpr (NL == 0) {
     // 16-slot pool: pool slot i (lane i) meets batch slot B-16+i, which is
     // lane 16+i of the last batch register.
@@ -232,8 +239,7 @@ __device__ __forceinline__ void merge_pool(float (&pd)[pool_regs(NL)], int (&pi)
       pd[0] = od;
       pi[0] = oi;
     }
-#pragma unroll
-    for (int sub = 8; sub >= 1; sub >>= 1) cx_lanes(pd[0], pi[0], sub, false, lane);
+    half_clean<0>(pd, pi, lane);
   } else {
     constexpr int NC = NL < NB ? NL : NB;
 #pragma unroll
@@ -246,21 +252,7 @@ __device__ __forceinline__ void merge_pool(float (&pd)[pool_regs(NL)], int (&pi)
         pi[pr] = bi[br];
       }
     }
-    constexpr int L = 32 * NL;
-#pragma unroll
-    for (int sub = L / 2; sub >= 1; sub >>= 1) {
-      if (sub >= 32) {
-        const int rs = sub >> 5;
-#pragma unroll
-        for (int j = 0; j < NL; ++j) {
-          if (j & rs) continue;
-          cx_regs(pd[j], pi[j], pd[j + rs], pi[j + rs], false);
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < NL; ++j) cx_lanes(pd[j], pi[j], sub, false, lane);
-      }
-    }
+    half_clean<NL>(pd, pi, lane);
   }
 }
 
@@ -281,6 +273,74 @@ __device__ __forceinline__ bool batch_can_enter(const float (&pd)[pool_regs(NL)]
 #pragma unroll
   for (int j = 0; j < batch_regs(NB); ++j) below |= bd[j] < pmax;
   return __any_sync(kFull, below);
+}
+
+// Candidates a batch may hold for merge_few.
+constexpr int kFewMax = 8;
+
+// Main-loop merge of a batch in which only a few slots (the candidates) hold
+// distances below the pool's largest, pmax.
+// The descending batch sort puts those candidates, if their distances are
+// pairwise distinct, in the batch's last slots in descending order whatever
+// the network does with the other slots: the candidate of ascending rank r
+// lands in batch slot B-1-r, which the merge pairs with pool slot L-1-r.
+// Every other batch slot holds a distance >= the pool's largest, so its
+// comparison (pool > batch, strict) takes nothing.  Placing each candidate
+// against pool slot L-1-r by its rank and running the half-cleaner therefore
+// gives exactly the network's pool.  Returns false, changing nothing, when
+// two candidates tie (the network's order of equal distances then decides
+// which id lands where, so the caller runs it).
+template <int NL, int NB>
+__device__ __forceinline__ bool merge_few(float (&pd)[pool_regs(NL)], int (&pi)[pool_regs(NL)],
+                                          const float (&bd)[batch_regs(NB)], const int (&bi)[batch_regs(NB)],
+                                          float pmax, int lane) {
+  constexpr int BR = batch_regs(NB), PR = pool_regs(NL), L = pool_slots(NL);
+  unsigned cm[BR];
+#pragma unroll
+  for (int j = 0; j < BR; ++j) cm[j] = __ballot_sync(kFull, bd[j] < pmax);
+  // ascending rank of this lane's candidate in batch register t, 4 bits
+  // at bit 4t (ranks stay below kFewMax = 8; BR <= 8)
+  unsigned rank = 0;
+  bool tie = false;
+#pragma unroll
+  for (int j = 0; j < BR; ++j) {
+    unsigned mask = cm[j];
+    while (mask) {
+      const int src = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const float v = __shfl_sync(kFull, bd[j], src);
+#pragma unroll
+      for (int t = 0; t < BR; ++t) {
+        if ((cm[t] >> lane) & 1u) {
+          rank += bd[t] > v ? 1u << (4 * t) : 0u;
+          tie |= bd[t] == v && !(t == j && lane == src);
+        }
+      }
+    }
+  }
+  if (__any_sync(kFull, tie)) return false;
+#pragma unroll
+  for (int j = 0; j < BR; ++j) {
+    unsigned mask = cm[j];
+    while (mask) {
+      const int src = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const float v = __shfl_sync(kFull, bd[j], src);
+      const int id = __shfl_sync(kFull, bi[j], src);
+      const int slot = L - 1 - (int)((__shfl_sync(kFull, rank, src) >> (4 * j)) & 15u);
+      if (lane == (slot & 31) && v != kMaxDist) {  // the main loop never takes a MAX slot
+#pragma unroll
+        for (int p = 0; p < PR; ++p) {
+          if (p == (slot >> 5) && pd[p] > v) {
+            pd[p] = v;
+            pi[p] = id;
+          }
+        }
+      }
+    }
+  }
+  half_clean<NL>(pd, pi, lane);
+  return true;
 }
 
 // Partial sum of one lane for one row: s = t0*t0, then fmaf(tc, tc, s) over
@@ -942,9 +1002,22 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     }
 
     c_dists += batch_distances<C, NB, PREC>(a, qv, qx, bd, bi, s_ids, s_dist, lane);
-    if (batch_can_enter<NL, NB>(pd, bd)) {
-      sort_batch_desc<BR, true, B, kMergeFrom>(bd, bi, lane);
-      merge_pool<NL, NB>(pd, pi, bd, bi, true, lane);
+    {
+      // batch slots below the pool's largest distance: none -> the merge
+      // changes nothing (batch_can_enter); a few distinct ones -> placed
+      // by rank (merge_few); otherwise the reference's network
+      const float pmax = __shfl_sync(kFull, pd[PR - 1], NL == 0 ? 15 : 31);
+      int m = 0;
+      bool nan = false;
+#pragma unroll
+      for (int j = 0; j < BR; ++j) {
+        m += __popc(__ballot_sync(kFull, bd[j] < pmax));
+        nan |= bd[j] != bd[j];
+      }
+      if (m > 0 && (m > kFewMax || __any_sync(kFull, nan) || !merge_few<NL, NB>(pd, pi, bd, bi, pmax, lane))) {
+        sort_batch_desc<BR, true, B, kMergeFrom>(bd, bi, lane);
+        merge_pool<NL, NB>(pd, pi, bd, bi, true, lane);
+      }
     }
 
     bool any = false;

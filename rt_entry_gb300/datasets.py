@@ -186,44 +186,94 @@ def knn_graph_fast(base: np.ndarray, R: int, device: str | None = None) -> np.nd
                                     device=dev.index or 0))
 
 
+def _exact_row(base, i, cols, R):
+    """Row i's R nearest of the candidate columns by exact FP64 (distance, id),
+    self excluded."""
+    cols = cols[cols != i]
+    dd = ((base[cols].astype(np.float64) - base[i].astype(np.float64)) ** 2).sum(-1)
+    o = np.lexsort((cols, dd))
+    return cols[o[:R]]
+
+
+def _boundary_rows(D, kth, tol, kk):
+    """Rows (of a block of approximate distances D) where more than kk
+    columns lie within 2*tol of the kk-th smallest: ties or near-ties that
+    cross the candidate cut, which those rows settle over every such column.
+    Elsewhere every column whose exact distance can reach the R-th (R <= kk)
+    is among the kk kept: its approximate distance is at most the R-th's
+    approximate distance plus 2*tol."""
+    return np.nonzero((D <= (kth + 2 * tol)[:, None]).sum(1) > kk)[0]
+
+
 def knn_graph(base: np.ndarray, R: int, device: str | None = None, chunk: int = 4096) -> np.ndarray:
-    """Exact degree-R kNN graph (self excluded), rows ordered by (dist, id)."""
-    n = base.shape[0]
+    """Exact degree-R kNN graph (self excluded), rows ordered by (dist, id).
+    Candidates come from approximate distances |x|^2 + |y|^2 - 2 x.y (FP32 on
+    a device, FP64 on the host) with a bound tol on their error; rows whose
+    candidate cut falls inside a run of (near-)equal distances are redone
+    over the whole run, so many equal distances (duplicated rows) still give
+    the smallest ids."""
+    n, d = base.shape
     if n <= R:
         raise ValueError("need more than R base vectors")
     torch, dev = _torch_device(device)
     extra = 8
+    kk = R + extra
     out = np.empty((n, R), np.int32)
     if dev is not None:
         prev = torch.backends.cuda.matmul.allow_tf32
         torch.backends.cuda.matmul.allow_tf32 = False
         try:
             X = torch.from_numpy(base).to(dev)
-            nrm = (X.double() ** 2).sum(1).float()
+            nrm64 = (X.double() ** 2).sum(1)
+            nrm_d = nrm64.float()
+            nmax = float(nrm64.max())
             for s in range(0, n, chunk):
                 e = min(n, s + chunk)
-                D = nrm[s:e, None] + nrm[None, :] - 2.0 * (X[s:e] @ X.T)
+                D = nrm_d[s:e, None] + nrm_d[None, :] - 2.0 * (X[s:e] @ X.T)
                 D[torch.arange(e - s, device=dev), torch.arange(s, e, device=dev)] = float("inf")
-                dv, iv = torch.topk(D, R + extra, dim=1, largest=False)
+                dv, iv = torch.topk(D, kk, dim=1, largest=False)
                 # exact FP64 distances of the candidates, then (dist, id) order
-                cand = X[iv.reshape(-1)].reshape(e - s, R + extra, -1).double()
+                cand = X[iv.reshape(-1)].reshape(e - s, kk, -1).double()
                 dd = ((cand - X[s:e, None, :].double()) ** 2).sum(-1)
                 dd_np, iv_np = _sort_by_dist_then_id(dd.cpu().numpy(), iv.cpu().numpy())
                 out[s:e] = iv_np[:, :R]
+                # FP32 products and sums: error below (d + 2) 2^-22 (|x|^2 + |y|^2);
+                # the cut at kth + 4 tol leaves room for its own FP32 rounding
+                tol = ((d + 2) * 2.0 ** -22 * (nrm64[s:e] + nmax)).float()
+                thr = dv[:, -1] + 4 * tol
+                cnt = (D <= thr[:, None]).sum(1)
+                over = (cnt > kk).nonzero().flatten()
+                if over.numel():  # redo those rows over every column below the cut
+                    kb = int(cnt[over].max())
+                    step = max(1, min(256, (1 << 30) // (kb * d * 8)))
+                    for o0 in range(0, over.numel(), step):
+                        sub = over[o0:o0 + step]
+                        _, ivb = torch.topk(D[sub], kb, dim=1, largest=False)
+                        xb = X[ivb.reshape(-1)].reshape(sub.numel(), kb, -1).double()
+                        ddb = ((xb - X[s + sub, None, :].double()) ** 2).sum(-1)
+                        _, ivb = _gpu_sort_dist_id(ddb, ivb)
+                        out[(s + sub).cpu().numpy()] = ivb[:, :R].cpu().numpy()
         finally:
             torch.backends.cuda.matmul.allow_tf32 = prev
         return out
-    X = base.astype(np.float64)
-    nrm = (X ** 2).sum(1)
+    X64 = base.astype(np.float64)
+    nrm = (X64 ** 2).sum(1)
+    nmax = float(nrm.max())
     for s in range(0, n, 1024):
         e = min(n, s + 1024)
-        D = nrm[s:e, None] + nrm[None, :] - 2.0 * (X[s:e] @ X.T)
+        D = nrm[s:e, None] + nrm[None, :] - 2.0 * (X64[s:e] @ X64.T)
         D[np.arange(e - s), np.arange(s, e)] = np.inf
-        iv = np.argpartition(D, R + extra, axis=1)[:, :R + extra]
-        cand = X[iv]
-        dd = ((cand - X[s:e, None, :]) ** 2).sum(-1)
-        _, iv = _sort_by_dist_then_id(dd, iv)
-        out[s:e] = iv[:, :R]
+        iv = np.argpartition(D, kk, axis=1)[:, :kk]
+        cand = X64[iv]
+        dd = ((cand - X64[s:e, None, :]) ** 2).sum(-1)
+        _, iv2 = _sort_by_dist_then_id(dd, iv)
+        out[s:e] = iv2[:, :R]
+        # FP64 products and sums: error below (d + 2) 2^-50 (|x|^2 + |y|^2)
+        tol = (d + 2) * 2.0 ** -50 * (nrm[s:e] + nmax)
+        kth = np.take_along_axis(D, iv, 1).max(1)
+        for r in _boundary_rows(D, kth, tol, kk):
+            cols = np.nonzero(D[r] <= kth[r] + 2 * tol[r])[0]
+            out[s + r] = _exact_row(base, s + r, cols, R)
     return out
 
 

@@ -38,3 +38,32 @@ def test_knn_graph_device_io_and_duplicates(lib, cuda):
     assert np.array_equal(g.cpu().numpy(), ds.knn_graph(base, 24, device="cpu"))
     with pytest.raises(r.RteError):
         r.knn_graph(base[:10], 10)  # degree must be below n
+
+
+def test_knn_graph_on_offset_high_dim_data(lib, cuda):
+    """Values in [0, 1] around 0.5 in 960 dimensions (the high-dimension
+    configuration's data): certified from the centred rows."""
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base = ds.make_config(3, n=3000, nq=10, with_graph=False, with_gt=False).base
+    assert base.min() >= 0.0 and base.max() <= 1.0 and abs(float(base.mean()) - 0.5) < 0.1
+    g = r.knn_graph(base, 64)
+    assert np.array_equal(g, ds.knn_graph(base, 64, device="cpu"))
+
+
+def test_knn_graph_retries_rows_with_many_equal_distances(lib, cuda, capfd, monkeypatch):
+    """300 copies of one row: each has 299 neighbours at distance 0, more
+    than the first pass's 2R + 32 candidates, so its R-th distance equals the
+    left-out bound and it is redone with 1024 candidates from the same block
+    of dot products."""
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base = _mixture(4000, 64, True, seed=11)
+    base[1000:1300] = base[1000]
+    monkeypatch.setenv("RTE_KNN_VERBOSE", "1")
+    g = r.knn_graph(base, 32)
+    import re
+    err = capfd.readouterr().err
+    m = re.search(r"(\d+) rows retried", err)
+    assert m and int(m.group(1)) >= 300, err
+    assert np.array_equal(g, ds.knn_graph(base, 32, device="cpu"))

@@ -122,6 +122,44 @@ def test_search_matches_oracle_sweep(lib, orc, cuda, d, integer, R, L, W, bw, nh
     assert np.array_equal(ids, ids2) and np.array_equal(dd, dd2)
 
 
+# A main-loop batch with 1..8 distances below the pool's largest, pairwise
+# distinct, is merged by rank; ties, NaN or more candidates take the
+# reference's sort-and-merge network.  "dup" repeats every row of the base's
+# second half from its first half (exact ties between candidates), "real" has
+# real-valued rows (distinct distances).
+MERGE_CASES = [
+    # d, degree, beam, width, data
+    (128, 64, 16, 1, "dup"),
+    (128, 64, 32, 1, "real"),
+    (128, 64, 64, 2, "dup"),
+    (128, 32, 128, 1, "real"),
+    (128, 16, 16, 1, "real"),   # 16-slot batch
+    (64, 16, 64, 2, "dup"),
+    (160, 32, 32, 1, "dup"),    # kernel built for any chunk count
+    (32, 32, 256, 2, "real"),
+]
+
+
+@pytest.mark.parametrize("d,R,L,W,kind", MERGE_CASES)
+def test_merge_by_rank_and_network_match_oracle(lib, orc, cuda, d, R, L, W, kind):
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(3000, 300, d, kind == "dup", seed=7 * d + L + W + R)
+    if kind == "dup":
+        rng = np.random.Generator(np.random.Philox(d + L))
+        base[1500:] = base[rng.integers(0, 1500, 1500)]
+    graph = ds.knn_graph(base, R)
+    idx = _index(base, graph, 24, 0.2)
+    _, _, pids = idx.kdtree()
+    hits = idx.locate(q)
+    ids, dd = idx.search_projected(q, beam=L, k=L, search_width=W)
+    oids, od, ocnt = orc.search(base, q, graph, L=L, k=L, search_width=W, leaf_pids=pids, hits=hits,
+                                with_counters=True)
+    merges, idle, few = ocnt[:, 4].sum(), ocnt[:, 5].sum(), ocnt[:, 6].sum()
+    assert few > 0 and merges - idle - few > 0, "both merge paths must occur"
+    assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
+    assert np.array_equal(dd, od)
+
+
 def test_topk_prefix_and_host_device_io(lib, orc, cuda):
     import torch
     from rt_entry_gb300 import datasets as ds

@@ -82,6 +82,14 @@ def test_oracle_pool_is_sorted_and_valid(orc):
     # a node; the idle ones (no batch distance below the pool's largest) are
     # a subset
     assert (cnt[:, 4] >= 1).all() and (cnt[:, 5] <= cnt[:, 4]).all() and (cnt[:, 5] > 0).any()
+    # main-loop merges with 1..8 distinct candidates: disjoint from the idle
+    # ones, and none at all when every base row is the same point (every
+    # candidate then ties with every other)
+    assert (cnt[:, 6] <= cnt[:, 4] - cnt[:, 5]).all() and (cnt[:, 6] > 0).any()
+    same = np.repeat(c["base"][:1], c["base"].shape[0], 0)
+    _, _, cs = orc.search(same, c["queries"], c["graph"], L=64, k=64, leaf_pids=c["leaf_pids"],
+                          hits=c["hits"], with_counters=True)
+    assert (cs[:, 6] == 0).all()
 
 
 def test_oracle_l2_matches_fp64_closely(orc):
