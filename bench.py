@@ -279,7 +279,15 @@ class Bench:
         the same launch) / its mean event time, against the measured copy
         bandwidth; frac_dram from an ncu capture's DRAM bytes when one exists."""
         steps, warmup = self.args.steps, self.args.warmup
+        # inside `rte_roof`, a range named by the key: a profiler filtering on
+        # rte_roof and renaming launches by their innermost range attributes
+        # each launch's DRAM bytes to its key
+        nvtx = self.torch.cuda.nvtx
+        nvtx.range_push("rte_roof")
+        nvtx.range_push(traffic_key or "search_kernel/unnamed")
         kms = statistics.mean(self.time_kernel(idx, qp, hits, params, steps, warmup))
+        nvtx.range_pop()
+        nvtx.range_pop()
         cnt = idx.counters(qp, hits=hits, params=params)
         prec = params.precision
         elem = 4 if prec == 0 else 2 if prec == 1 else 1
@@ -467,11 +475,11 @@ def measure_arm(B, idx, qd, gt, tune_q, tune_gt, d, R, name, **kw):
     ms = statistics.median(B.time_path(idx, qd, p, B.args.steps, B.args.warmup))
     qp = idx.project(qd)
     hits = idx.learned_leaves(qp) if kw.get("entry_mode") == r.ENTRY_LEARNED else idx.locate(qp)
-    roof = B.roofline(idx, qp, hits, p, d, R)
+    roof = B.roofline(idx, qp, hits, p, d, R, f"search_kernel/{name}/beam{L}/width{W}")
     nq = qd.shape[0]
     res = {"beam": L, "width": W, "met_0.95_on_held_out": met, "recall_at_10": round(rec, 4),
            "qps": round(nq / (ms / 1000.0)), "ms_per_step": round(ms, 4), "frac": roof["frac"],
-           "kernel_ms": roof["kernel_ms"]}
+           "frac_dram": roof["frac_dram"], "kernel_ms": roof["kernel_ms"]}
     B.details.setdefault("tune_curves", {})[name] = tcurve
     if not met:  # the whole scored curve, so the recall-QPS trade-off is on record
         B.details.setdefault("scored_curves", {})[name] = B.curve(idx, qd, gt, SWEEP, **kw)

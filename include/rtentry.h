@@ -67,6 +67,10 @@ typedef struct {
   int max_hits;      /* kd-tree entries from the first max_hits containing leaves (1..8;
                         the reference's max_hits, flags.cpp:100, multi-hit entry
                         entry_helper.cu:5-241); caller hits are then [nq x max_hits]  */
+  int team_warps;    /* warps that share one query's distance evaluations: 1, 2, 4 or 8
+                        (a multiple of warps_per_block), or 0 = automatic: the most, up
+                        to 8, that the batch leaves room for in the resident warps, so a
+                        small batch still fills the GPU.  Results do not depend on it.  */
 } rte_search_params;
 
 typedef struct {

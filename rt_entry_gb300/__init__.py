@@ -43,7 +43,8 @@ class SearchParams(ctypes.Structure):
                 ("max_iter", ctypes.c_int), ("bloom_words", ctypes.c_int),
                 ("bloom_hashes", ctypes.c_int), ("precision", ctypes.c_int),
                 ("rerank", ctypes.c_int), ("entry_mode", ctypes.c_int),
-                ("warps_per_block", ctypes.c_int), ("max_hits", ctypes.c_int)]
+                ("warps_per_block", ctypes.c_int), ("max_hits", ctypes.c_int),
+                ("team_warps", ctypes.c_int)]
 
 
 class IndexInfo(ctypes.Structure):

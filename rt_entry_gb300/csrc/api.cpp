@@ -199,9 +199,24 @@ int next_pow2(int v) {
 }
 
 struct Plan {
-  int L, k, NL, NB, wpb, grid, prec;
+  int L, k, NL, NB, wpb, grid, prec, team;
   size_t smem;
 };
+
+}  // namespace
+
+namespace rte {
+// The fewest warps per query that automatic teams use.  FP32 rows with pools
+// of up to 64 slots: their gathers bound the search, and two warps per query
+// keep twice the rows in flight, which is faster even when the batch fills
+// the GPU (measured on one GB300 at 10k and 40k queries: 9-17 % at beams
+// 16 to 64; no gain at 128 and 256, nor for BF16 or FP8 rows).
+int team_floor(int prec, int L, int wpb) {
+  return prec == kPrecF32 && L <= 64 && wpb % 2 == 0 ? 2 : 1;
+}
+}  // namespace rte
+
+namespace {
 
 rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t nq, Plan& pl) {
   if (!prm) return fail(RTE_EINVAL, "params is NULL");
@@ -224,6 +239,9 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
   if (prm->max_hits < 1 || prm->max_hits > kMaxHits) return fail(RTE_EINVAL, "max_hits must be in [1, 8]");
   if (prm->max_hits > 1 && prm->entry_mode != RTE_ENTRY_KDTREE)
     return fail(RTE_EINVAL, "max_hits > 1 needs kd-tree entries");
+  if (prm->team_warps != 0 && prm->team_warps != 1 && prm->team_warps != 2 && prm->team_warps != 4 &&
+      prm->team_warps != 8)
+    return fail(RTE_EINVAL, "team_warps must be 0, 1, 2, 4 or 8");
   if (prm->entry_mode < RTE_ENTRY_RANDOM || prm->entry_mode > RTE_ENTRY_LEARNED)
     return fail(RTE_EINVAL, "entry_mode must be RTE_ENTRY_RANDOM, _KDTREE or _LEARNED");
   if (prm->entry_mode == RTE_ENTRY_LEARNED && !x->mlp.trained)
@@ -240,13 +258,20 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
   const int S = std::max(B, pl.L);
   const bool r16 = x->degree == 16;
   const int kc = search_kernel_chunks(x->C, pl.NL, pl.NB, pl.prec, r16);
-  const size_t per_warp = (size_t)(prm->bloom_words + 2 * S + query_slot_words_for(kc, x->C)) * 4;
+  const size_t per_warp =
+      (size_t)(prm->bloom_words + 2 * S + query_slot_words_for(kc, x->C) + kTeamCtlWords) * 4;
   const size_t smem_cap = 227 * 1024;
+  const int team = prm->team_warps;
   if (prm->warps_per_block > 0) {
     pl.wpb = prm->warps_per_block;
     if (pl.wpb > 8) return fail(RTE_EINVAL, "warps_per_block must be <= 8");
+    if (team > 1 && pl.wpb % team != 0)
+      return fail(RTE_EINVAL, "warps_per_block must be a multiple of team_warps");
   } else {
     pl.wpb = (int)std::min<size_t>(8, smem_cap / per_warp);
+    if (team > 1) pl.wpb -= pl.wpb % team;  // whole teams per block
+    if (team > 1 && pl.wpb < team)
+      return fail(RTE_EINVAL, "the bloom filter leaves room for fewer warps per block than team_warps");
   }
   pl.smem = (size_t)pl.wpb * per_warp;
   if (pl.wpb < 1 || pl.smem > smem_cap)
@@ -255,7 +280,13 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
   if (occ <= 0)
     return fail(RTE_EINVAL, "no kernel instantiation for beam " + std::to_string(pl.L) + ", batch " +
                                 std::to_string(B) + ", precision " + std::to_string(pl.prec));
-  const int64_t need = (nq + pl.wpb - 1) / pl.wpb;
+  const int64_t resident = (int64_t)x->num_sms * occ * pl.wpb;  // warps
+  pl.team = team;
+  if (team == 0) {  // automatic: spread a small batch's queries over the idle warps
+    pl.team = team_floor(pl.prec, pl.L, pl.wpb);
+    while (pl.team < 8 && pl.wpb % (2 * pl.team) == 0 && nq * 2 * pl.team <= resident) pl.team *= 2;
+  }
+  const int64_t need = (nq * pl.team + pl.wpb - 1) / pl.wpb;
   pl.grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)x->num_sms * occ));
   return RTE_OK;
 }
@@ -428,6 +459,7 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   a.rerank = full_rerank ? 0 : prm->rerank;
   a.n_leaves = x->has_kdtree ? (int)x->kd.n_leaves : 1;
   a.max_hits = prm->max_hits;
+  a.team = pl.team;
   RTE_CUDA(launch_search(a, x->C, pl.NL, pl.NB, pl.prec, pl.wpb, pl.grid, pl.smem, st));
   if (full_rerank)
     RTE_CUDA(launch_rerank_full(x->raw.p, x->np, x->dim, d_queries, x->dim, poolb.as<int32_t>(),
@@ -440,10 +472,11 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
 namespace rte {
 // Launch plan of a search, for entry points defined in other files.
 rte_status search_plan(const rte_index* x, const rte_search_params* prm, int64_t nq, int* L, int* k,
-                       int* NL, int* NB, int* wpb, int* grid, size_t* smem) {
+                       int* NL, int* NB, int* wpb, int* grid, size_t* smem, int* team) {
   Plan pl;
   rte_status s = plan_search(x, prm, nq, pl);
   if (s != RTE_OK) return s;
+  *team = pl.team;
   *L = pl.L;
   *k = pl.k;
   *NL = pl.NL;
@@ -480,6 +513,7 @@ void rte_default_params(rte_search_params* p) {
   p->entry_mode = RTE_ENTRY_KDTREE;
   p->warps_per_block = 0;
   p->max_hits = 1;
+  p->team_warps = 0;
 }
 
 const char* rte_last_error(void) { return g_err.c_str(); }

@@ -23,7 +23,7 @@
 
 namespace rte {
 rte_status search_plan(const rte_index* x, const rte_search_params* prm, int64_t nq, int* L, int* k,
-                       int* NL, int* NB, int* wpb, int* grid, size_t* smem);
+                       int* NL, int* NB, int* wpb, int* grid, size_t* smem, int* team);
 }  // namespace rte
 
 using namespace rte;
@@ -92,9 +92,9 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   DeviceGuard guard(x->device);
   // parameters are validated before an empty batch returns, as
   // rte_search_projected does
-  int L, k, NL, NB, wpb, grid;
+  int L, k, NL, NB, wpb, grid, team;
   size_t smem;
-  rte_status s = search_plan(x, params, nq, &L, &k, &NL, &NB, &wpb, &grid, &smem);
+  rte_status s = search_plan(x, params, nq, &L, &k, &NL, &NB, &wpb, &grid, &smem, &team);
   if (s != RTE_OK) return s;
   if (params->rerank == 2)
     return fail(RTE_EINVAL, "rerank 2 needs the original queries: use rte_search");
@@ -150,6 +150,7 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   a.rerank = params->rerank;
   a.n_leaves = x->has_kdtree ? (int)x->kd.n_leaves : 1;
   a.max_hits = 1;
+  a.team = team;
   RTE_CUDA(launch_search(a, x->C, NL, NB, params->precision, wpb, grid, smem, st));
   return RTE_OK;
 }

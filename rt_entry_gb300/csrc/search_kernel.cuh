@@ -392,6 +392,25 @@ __device__ __forceinline__ float lane_partial(const float (&p)[C], const float (
 }
 
 // ---- BF16 distances on the tensor cores (rows of 32*C <= 128 dims) ----
+// A team: K warps of one block that serve one query (search_kernel_team).
+// The leader (w == 0)
+// runs the search; at each distance phase it publishes the row count in
+// ctl[1] and the K warps each compute an interleaved share of the row groups
+// into the leader's compaction buffers, between two crossings of the team's
+// named barrier.  ctl[0] carries the team's query, ctl[1] = -1 ends it.
+// Named barriers are hardware waits that every member reaches on every path,
+// so a team needs no spin-wait.
+struct Team {
+  int K = 1;                     // warps per query
+  int w = 0;                     // this warp's index in the team
+  int bar = 0;                   // named barrier id (1 + team index in the block)
+  volatile int* ctl = nullptr;   // [0] query, [1] phase: row count (+ 1<<16 for the rerank), -1 = done
+};
+
+__device__ __forceinline__ void team_sync(const Team& t) {
+  asm volatile("bar.sync %0, %1;" ::"r"(t.bar), "r"(32 * t.K) : "memory");
+}
+
 // dist = |p|^2 + |q|^2 - 2 p.q, p the BF16 row, q the query rounded to BF16,
 // p.q from mma.sync m16n8k16 (BF16 inputs, exact products, FP32
 // accumulation).  A BF16 row (32*C values, 64*C bytes) is read as C pieces
@@ -457,18 +476,39 @@ __device__ __forceinline__ void prefetch_rows(const char* rows, const int* s_ids
   }
 }
 
+// The same for the rows of a team member's share: groups of G rows, group
+// g belonging to member g % K.  lines = 128-byte lines per row.
+template <int G>
+__device__ __forceinline__ void prefetch_share(const char* rows, size_t row_bytes, int lines,
+                                               const int* s_ids, int n, int lane, int w, int K) {
+  const int per = G * lines;
+  for (int i = lane;; i += 32) {
+    const int j = i / per;
+    const int g0 = G * (w + j * K);
+    if (g0 >= n) break;
+    const int r = i - j * per;
+    const int row = g0 + r / lines;
+    if (row < n)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(rows + (size_t)s_ids[row] * row_bytes + (r % lines) * 128));
+  }
+}
+
 // Distances of the n ids in s_ids[0..n) by the tensor cores, 8 rows per MMA
 // group: thread (g, t) supplies row g of the group as column g of the MMA's
 // B operand; the query is every row of A, so D[.][col] is the dot product of
 // row col, and lanes 0..3 hold the group's eight results.
-template <int C>
+template <int C, bool TEAM>
 __device__ __forceinline__ void distances_mma(const SearchArgs& a, const QueryExtra<C, kPrecBF16, true>& qx,
-                                              const int* s_ids, float* s_dist, int n, int lane) {
+                                              const int* s_ids, float* s_dist, int n, int lane, int w, int K) {
   constexpr int kRowBytes = 64 * C;
   const char* rows = reinterpret_cast<const char*>(a.base_bf16);
-  prefetch_rows<kRowBytes>(rows, s_ids, n, lane);
+  if constexpr (TEAM)
+    prefetch_share<8>(rows, kRowBytes, (kRowBytes + 127) / 128, s_ids, n, lane, w, K);
+  else
+    prefetch_rows<kRowBytes>(rows, s_ids, n, lane);
   const int g = lane >> 2, t = lane & 3;
-  for (int r0 = 0; r0 < n; r0 += 8) {
+  const int first = TEAM ? 8 * w : 0, step = TEAM ? 8 * K : 8;
+  for (int r0 = first; r0 < n; r0 += step) {
     const int ra = r0 + g;
     const int id = s_ids[ra < n ? ra : r0];
     const char* p = rows + (size_t)id * kRowBytes + 16 * t;
@@ -597,9 +637,9 @@ __device__ __forceinline__ void reduce_rows(float (&part)[G], float* s_dist, int
 
 // Distances of n rows of a.C chunks against the query row in shared memory
 // qs (interleaved layout), G rows in flight.
-template <int PREC>
+template <int PREC, bool TEAM>
 __device__ __forceinline__ void distances_rt(const SearchArgs& a, const float* qs, const int* s_ids,
-                                             float* s_dist, int n, int lane) {
+                                             float* s_dist, int n, int lane, int w, int K) {
   constexpr int G = 4;
   const int C = a.C, n4 = C >> 2, rem = C & 3;
   const size_t stride = 32 * (size_t)C;  // elements per row
@@ -609,12 +649,17 @@ __device__ __forceinline__ void distances_rt(const SearchArgs& a, const float* q
                        : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
                                            : reinterpret_cast<const char*>(a.base_fp8);
     const size_t rb = stride * SlabLoader<PREC>::kBytes;
-    for (int i = lane; i < n * lines; i += 32) {
-      const int row = i / lines, line = i - row * lines;
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(rows + (size_t)s_ids[row] * rb + line * 128));
+    if constexpr (TEAM) {
+      prefetch_share<G>(rows, rb, lines, s_ids, n, lane, w, K);
+    } else {
+      for (int i = lane; i < n * lines; i += 32) {
+        const int row = i / lines, line = i - row * lines;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(rows + (size_t)s_ids[row] * rb + line * 128));
+      }
     }
   }
-  for (int g0 = 0; g0 < n; g0 += G) {
+  const int first = TEAM ? G * w : 0, step = TEAM ? G * K : G;
+  for (int g0 = first; g0 < n; g0 += step) {
     SlabLoader<PREC> r[G];
 #pragma unroll
     for (int t = 0; t < G; ++t) r[t].init(a, s_ids[g0 + t < n ? g0 + t : g0], stride);
@@ -665,14 +710,15 @@ __device__ __forceinline__ void distances_rt(const SearchArgs& a, const float* q
 // finish the sum, which lands in the 32/G lanes lane = t*(32/G) + ...
 // Every addition pairs the same two partial sums as the reference's
 // shuffle-down tree (addition is commutative, so the results are equal).
-template <int C, int PREC>
+// With TEAM, the groups of rows of member w of a K-warp team only.
+template <int C, int PREC, bool TEAM = false>
 __device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)[qregs(C)],
                                           const QueryExtra<C, PREC>& qx, const int* s_ids,
-                                          float* s_dist, int n, int lane) {
+                                          float* s_dist, int n, int lane, int w = 0, int K = 1) {
   if constexpr (C == 0) {
-    distances_rt<PREC>(a, qx.qs, s_ids, s_dist, n, lane);
+    distances_rt<PREC, TEAM>(a, qx.qs, s_ids, s_dist, n, lane, w, K);
   } else if constexpr (PREC == kPrecBF16 && C <= 4) {
-    distances_mma<C>(a, qx, s_ids, s_dist, n, lane);
+    distances_mma<C, TEAM>(a, qx, s_ids, s_dist, n, lane, w, K);
   } else {
     constexpr int G = C <= 4 ? 8 : 2;
     {
@@ -680,9 +726,13 @@ __device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)
       const char* rows = PREC == kPrecF32    ? reinterpret_cast<const char*>(a.base)
                          : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
                                              : reinterpret_cast<const char*>(a.base_fp8);
-      prefetch_rows<kRowBytes>(rows, s_ids, n, lane);
+      if constexpr (TEAM)
+        prefetch_share<G>(rows, kRowBytes, (kRowBytes + 127) / 128, s_ids, n, lane, w, K);
+      else
+        prefetch_rows<kRowBytes>(rows, s_ids, n, lane);
     }
-    for (int g0 = 0; g0 < n; g0 += G) {
+    const int first = TEAM ? G * w : 0, step = TEAM ? G * K : G;
+    for (int g0 = first; g0 < n; g0 += step) {
       // all G loads first, unconditionally (a short group re-reads its first
       // row), so they are issued back to back before any use
       RowLoader<C, PREC> r[G];
@@ -698,12 +748,13 @@ __device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)
 
 // Compact the valid batch ids (0 <= id < np) into s_ids in slot order,
 // compute their distances, and scatter them back (invalid slots -> MAX).
-template <int C, int NB, int PREC>
+// With TEAM, the team's warps share the distances (team leader only).
+template <int C, int NB, int PREC, bool TEAM = false>
 __device__ __forceinline__ int batch_distances(const SearchArgs& a, const float (&qv)[qregs(C)],
                                                const QueryExtra<C, PREC>& qx,
                                                float (&bd)[batch_regs(NB)],
                                                const int (&bi)[batch_regs(NB)], int* s_ids,
-                                               float* s_dist, int lane) {
+                                               float* s_dist, int lane, const Team& t = Team()) {
   constexpr int BR = batch_regs(NB);
   const unsigned lt = (1u << lane) - 1u;
   int kidx[BR];
@@ -716,9 +767,16 @@ __device__ __forceinline__ int batch_distances(const SearchArgs& a, const float 
     if (v) s_ids[kidx[j]] = bi[j];
     n += __popc(m);
   }
-  __syncwarp();
-  distances<C, PREC>(a, qv, qx, s_ids, s_dist, n, lane);
-  __syncwarp();
+  if constexpr (TEAM) {
+    if (lane == 0) t.ctl[1] = n;
+    team_sync(t);
+    distances<C, PREC, true>(a, qv, qx, s_ids, s_dist, n, lane, 0, t.K);
+    team_sync(t);
+  } else {
+    __syncwarp();
+    distances<C, PREC>(a, qv, qx, s_ids, s_dist, n, lane);
+    __syncwarp();
+  }
 #pragma unroll
   for (int j = 0; j < BR; ++j) bd[j] = kidx[j] >= 0 ? s_dist[kidx[j]] : kMaxDist;
   __syncwarp();
@@ -731,11 +789,11 @@ __device__ __forceinline__ int batch_distances(const SearchArgs& a, const float 
 // the FP32 path computes them, then the pool is bitonic-sorted ascending.
 // The reference's precedent is the host-side parallel_reorder
 // (graph_helper.cu:146-213), which recomputes FP32 L2 and std::sorts.
-template <int C, int NL>
+template <int C, int NL, bool TEAM = false>
 __device__ __forceinline__ void rerank_pool(const SearchArgs& a, const float (&qv)[qregs(C)],
                                             const float* qsm, float (&pd)[pool_regs(NL)],
                                             int (&pi)[pool_regs(NL)], int* s_ids, float* s_dist,
-                                            int lane) {
+                                            int lane, const Team& t = Team()) {
   constexpr int PR = pool_regs(NL);
   const unsigned lt = (1u << lane) - 1u;
   int kidx[PR];
@@ -749,11 +807,18 @@ __device__ __forceinline__ void rerank_pool(const SearchArgs& a, const float (&q
     if (v) s_ids[kidx[j]] = pi[j];
     n += __popc(m);
   }
-  __syncwarp();
   QueryExtra<C, kPrecF32> q32{};
   if constexpr (C == 0) q32.qs = qsm;
-  distances<C, kPrecF32>(a, qv, q32, s_ids, s_dist, n, lane);
-  __syncwarp();
+  if constexpr (TEAM) {
+    if (lane == 0) t.ctl[1] = n | (1 << 16);
+    team_sync(t);
+    distances<C, kPrecF32, true>(a, qv, q32, s_ids, s_dist, n, lane, 0, t.K);
+    team_sync(t);
+  } else {
+    __syncwarp();
+    distances<C, kPrecF32>(a, qv, q32, s_ids, s_dist, n, lane);
+    __syncwarp();
+  }
 #pragma unroll
   for (int j = 0; j < PR; ++j) pd[j] = kidx[j] >= 0 ? s_dist[kidx[j]] : kMaxDist;
   __syncwarp();
@@ -765,26 +830,13 @@ __device__ __forceinline__ void rerank_pool(const SearchArgs& a, const float (&q
 // neighbour list.  For R >= 32 a node's list fills R / 32 whole registers
 // (register j holds node j / (R / 32)); R16 kernels serve degree-16 graphs,
 // whose lists fill half a register (slot p holds node p / 16).
-template <int C, int NL, int NB, int PREC, bool R16>
-__device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& bloom, int* s_ids,
-                             float* s_dist, uint32_t* q_slot) {
-  constexpr int L = pool_slots(NL);
-  constexpr int PR = pool_regs(NL);  // pool registers
-  constexpr int BR = batch_regs(NB);  // batch registers
-  // the merge reads batch registers BR - min(PR, BR) .. BR-1 only
-  constexpr int kMergeFrom = BR - (PR < BR ? PR : BR);
-  constexpr int B = batch_slots(NB);
-  static_assert(R16 || NB > 0, "a 16-slot batch comes from a degree-16 graph");
-  const int np = a.np;
-  const int R = R16 ? 16 : a.R;
-  const int NR = R >> 5;               // batch registers per node (R >= 32)
-  const int nr_shift = __ffs(NR) - 1;  // j / NR == j >> nr_shift
-  int c_entries = 0, c_expanded = 0, c_dists = 0;  // per query: far below 2^31
-
-  float qv[qregs(C)];
-  QueryExtra<C, PREC> qx;
+// The query's registers and shared-memory slot: FP32 chunks in registers
+// (C > 0; plus its BF16 row in q_slot for the tensor-core distances), or the
+// FP32 row in q_slot in the base's interleaved layout (C == 0).
+template <int C, int PREC>
+__device__ __forceinline__ void load_query(const SearchArgs& a, int q, int lane, float (&qv)[qregs(C)],
+                                           QueryExtra<C, PREC>& qx, uint32_t* q_slot) {
   if constexpr (C == 0) {
-    // the query row in the warp's shared memory, interleaved like the base
     float* qs = reinterpret_cast<float*>(q_slot);
     for (int c = 0; c < a.C; ++c) {
       const int dim = lane + 32 * c;
@@ -801,6 +853,28 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     }
     if constexpr (PREC == kPrecBF16 && C <= 4) make_query_extra<C>(qx, qv, q_slot, lane);
   }
+}
+
+template <int C, int NL, int NB, int PREC, bool R16, bool TEAM = false>
+__device__ __forceinline__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& bloom,
+                                             int* s_ids, float* s_dist, uint32_t* q_slot,
+                                             const Team& t = Team()) {
+  constexpr int L = pool_slots(NL);
+  constexpr int PR = pool_regs(NL);  // pool registers
+  constexpr int BR = batch_regs(NB);  // batch registers
+  // the merge reads batch registers BR - min(PR, BR) .. BR-1 only
+  constexpr int kMergeFrom = BR - (PR < BR ? PR : BR);
+  constexpr int B = batch_slots(NB);
+  static_assert(R16 || NB > 0, "a 16-slot batch comes from a degree-16 graph");
+  const int np = a.np;
+  const int R = R16 ? 16 : a.R;
+  const int NR = R >> 5;               // batch registers per node (R >= 32)
+  const int nr_shift = __ffs(NR) - 1;  // j / NR == j >> nr_shift
+  int c_entries = 0, c_expanded = 0, c_dists = 0;  // per query: far below 2^31
+
+  float qv[qregs(C)];
+  QueryExtra<C, PREC> qx;
+  load_query<C, PREC>(a, q, lane, qv, qx, q_slot);
 
   float pd[PR];
   int pi[PR];
@@ -864,7 +938,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
       bi[j] = id;
     }
     __syncwarp();
-    c_entries += batch_distances<C, NB, PREC>(a, qv, qx, bd, bi, s_ids, s_dist, lane);
+    c_entries += batch_distances<C, NB, PREC, TEAM>(a, qv, qx, bd, bi, s_ids, s_dist, lane, t);
     if (batch_can_enter<NL, NB>(pd, bd)) {
       sort_batch_desc<BR, true, B, kMergeFrom>(bd, bi, lane);
       merge_pool<NL, NB>(pd, pi, bd, bi, false, lane);
@@ -932,6 +1006,15 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
       }
     }
     if (nsel == 0) break;
+    // the next unvisited pool node, often the next iteration's choice: its
+    // adjacency row into L2 while this iteration's rows are gathered (the
+    // reduced-precision paths, which latency bounds; the FP32 path is
+    // bandwidth-bound and loses more to the prefetches that miss)
+    if (PREC != kPrecF32 && tmp_flag != 0) {
+      const int u = __shfl_sync(kFull, pick<PR>(pi, iteration), __ffs(tmp_flag) - 1);
+      if (u >= 0 && u < np && lane < ((R + 31) >> 5))
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(a.graph + (size_t)u * R + 32 * lane));
+    }
 
     // neighbour rows of the selected nodes (:995-1010); a node id >= np
     // expands nothing (the reference would read past the graph)
@@ -1001,7 +1084,7 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
       }
     }
 
-    c_dists += batch_distances<C, NB, PREC>(a, qv, qx, bd, bi, s_ids, s_dist, lane);
+    c_dists += batch_distances<C, NB, PREC, TEAM>(a, qv, qx, bd, bi, s_ids, s_dist, lane, t);
     {
       // batch slots below the pool's largest distance: none -> the merge
       // changes nothing (batch_can_enter); a few distinct ones -> placed
@@ -1047,7 +1130,11 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
 
   // ---- exact FP32 rerank of the final pool (precision paths) ----
   if (PREC != kPrecF32 && a.rerank)
-    rerank_pool<C, NL>(a, qv, reinterpret_cast<const float*>(q_slot), pd, pi, s_ids, s_dist, lane);
+    rerank_pool<C, NL, TEAM>(a, qv, reinterpret_cast<const float*>(q_slot), pd, pi, s_ids, s_dist, lane, t);
+  if constexpr (TEAM) {  // releases the helpers
+    if (lane == 0) t.ctl[1] = -1;
+    team_sync(t);
+  }
 
   // ---- output (:1959-1963) ----
 #pragma unroll
@@ -1064,6 +1151,31 @@ __device__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& 
     c[1] = c_expanded;
     c[2] = c_dists;
     c[3] = iter;
+  }
+}
+
+// A team member other than the leader, for one query: the query in its own
+// registers and slot, then its share of every distance phase the leader
+// opens, until the leader ends the query.
+template <int C, int PREC>
+__device__ __forceinline__ void help_query(const SearchArgs& a, int q, int lane, const int* s_ids,
+                                           float* s_dist, uint32_t* q_slot, const Team& t) {
+  float qv[qregs(C)];
+  QueryExtra<C, PREC> qx;
+  load_query<C, PREC>(a, q, lane, qv, qx, q_slot);
+  for (;;) {
+    team_sync(t);
+    const int code = t.ctl[1];
+    if (code < 0) break;
+    const int n = code & 0xffff;
+    if (code >> 16) {  // the exact FP32 rerank of the final pool
+      QueryExtra<C, kPrecF32> q32{};
+      if constexpr (C == 0) q32.qs = reinterpret_cast<const float*>(q_slot);
+      distances<C, kPrecF32, true>(a, qv, q32, s_ids, s_dist, n, lane, t.w, t.K);
+    } else {
+      distances<C, PREC, true>(a, qv, qx, s_ids, s_dist, n, lane, t.w, t.K);
+    }
+    team_sync(t);
   }
 }
 
@@ -1094,6 +1206,70 @@ __global__ void __launch_bounds__(256, (C <= 4 ? 4 : 2)) search_kernel(SearchArg
     if (q >= nq) break;
     search_query<C, NL, NB, PREC, R16>(a, q, lane, bloom, s_ids, s_dist,
                                        reinterpret_cast<uint32_t*>(s_dist + S));
+  }
+}
+
+// search_kernel with teams of K warps per query (Team): K = a.team, or,
+// for a.team < 0, at least -a.team and otherwise the most (up to 8) that the
+// live query count leaves room for in the grid.  K = 1 runs as a team of one.  A kernel of its own, so
+// that the single-warp kernel's code and register allocation stay as they
+// are; a team never spans blocks (the launch keeps warps per block a
+// multiple of K, and K falls back to 1 otherwise).
+template <int C, int NL, int NB, int PREC, bool R16 = false>
+__global__ void __launch_bounds__(256, (C <= 4 ? 4 : 2)) search_kernel_team(SearchArgs a) {
+  extern __shared__ uint32_t smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  constexpr int B = batch_slots(NB);
+  constexpr int S = B > pool_slots(NL) ? B : pool_slots(NL);
+  int qwords = kQuerySlotWords;
+  if constexpr (C == 0) qwords = query_slot_words_for(0, a.C);
+  // per warp: filter, compaction words, query slot, then the team's control
+  // words (used in the leader's region)
+  const int per_warp = a.bloom_words + 2 * S + qwords + kTeamCtlWords;
+  uint32_t* wbase = smem + (size_t)wib * per_warp;
+  Bloom bloom;
+  bloom.w = wbase;
+  bloom.words_mask = (uint32_t)a.bloom_words - 1u;
+  bloom.bits_mask = ((uint32_t)a.bloom_words << 5) - 1u;
+  bloom.lw = __ffs(a.bloom_words) - 1;
+  bloom.nh = a.bloom_hashes;
+  const int nq = a.nq_dev ? *a.nq_dev : a.nq;
+  const int wpb = blockDim.x >> 5;
+  int K = a.team;
+  if (K < 0) {  // at least -a.team warps, then as many as the live batch leaves room for
+    const long long total = (long long)gridDim.x * wpb;
+    K = -a.team;
+    while (K < 8 && wpb % (2 * K) == 0 && (long long)nq * 2 * K <= total) K *= 2;
+  }
+  if (K < 1 || K > 8 || wpb % K != 0) K = 1;
+  Team t;
+  t.K = K;
+  t.w = wib & (K - 1);
+  t.bar = 1 + wib / K;
+  uint32_t* lbase = smem + (size_t)(wib - t.w) * per_warp;  // the leader's region
+  t.ctl = reinterpret_cast<volatile int*>(lbase + per_warp - kTeamCtlWords);
+  int* ts_ids = reinterpret_cast<int*>(lbase + a.bloom_words);
+  float* ts_dist = reinterpret_cast<float*>(ts_ids + S);
+  // this warp's own query slot, after its filter and compaction words
+  uint32_t* own_slot = wbase + a.bloom_words + 2 * S;
+  if (t.w == 0) {
+    for (;;) {
+      int q = 0;
+      if (lane == 0) q = (int)atomicAdd(a.work, 1u);
+      q = __shfl_sync(kFull, q, 0);
+      if (lane == 0) t.ctl[0] = q;
+      team_sync(t);
+      if (q >= nq) break;
+      search_query<C, NL, NB, PREC, R16, true>(a, q, lane, bloom, ts_ids, ts_dist, own_slot, t);
+    }
+  } else {
+    for (;;) {
+      team_sync(t);
+      const int q = t.ctl[0];
+      if (q >= nq) break;
+      help_query<C, PREC>(a, q, lane, ts_ids, ts_dist, own_slot, t);
+    }
   }
 }
 

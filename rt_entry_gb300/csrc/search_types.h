@@ -13,14 +13,22 @@ enum : int { kPrecF32 = 0, kPrecBF16 = 1, kPrecFP8 = 2 };
 #endif
 
 // Shared memory of one warp of the search kernel, in 32-bit words: the bloom
-// filter, 2*max(batch, beam) compaction slots, and a slot for the query:
-// its BF16 row (tensor-core distances, up to 128 dims) in the kernels built
+// filter, 2*max(batch, beam) compaction slots, a slot for the query, and
+// (search_kernel_team) two control words.  The query slot holds
+// the query's BF16 row (tensor-core distances, up to 128 dims) in the kernels built
 // for one chunk count, or its FP32 row of `chunks` chunks in the kernels
 // built for any chunk count (kernel template C == 0).
 constexpr int kQuerySlotWords = 64;
 RTE_HD constexpr int query_slot_words_for(int C, int chunks) {
   return C == 0 ? (32 * chunks > kQuerySlotWords ? 32 * chunks : kQuerySlotWords) : kQuerySlotWords;
 }
+// Control words of a team (the query, the phase; two spare) at the end of
+// each warp's region in search_kernel_team; every launch reserves them.
+// Four words keep every region, and so every query slot, on a 16-byte
+// boundary: the query slot is read with 16-byte vector loads.  The filter
+// (a power of two >= 32 words), the compaction words (2 x 16..256) and the
+// query slot (64 or 32 x chunks words) are all multiples of 4 words.
+constexpr int kTeamCtlWords = 4;
 constexpr int kMaxHits = 8;  // leaves per query for kd-tree entries
 constexpr int kMaxChunks = 32;  // rows of up to 1024 dims
 
@@ -45,6 +53,8 @@ struct SearchArgs {
   int max_hits;             // entry mode 1: hits holds [nq][max_hits] leaves (-1 padded)
   const int* nq_dev;        // if set, the query count is read here (graph replay)
   int C;                    // chunks of 32 dims per row (set by launch_search)
+  int team;                 // warps per query: 0 or 1 alone, 2/4/8 a team, < 0 chosen
+                            // by the kernel from the live query count, at least -team
 };
 
 }  // namespace rte

@@ -31,7 +31,8 @@
 
 namespace rte {
 rte_status search_plan(const rte_index* x, const rte_search_params* prm, int64_t nq, int* L, int* k,
-                       int* NL, int* NB, int* wpb, int* grid, size_t* smem);
+                       int* NL, int* NB, int* wpb, int* grid, size_t* smem, int* team);
+int team_floor(int prec, int L, int wpb);
 }
 
 using namespace rte;
@@ -68,9 +69,9 @@ namespace {
 
 rte_status capture(rte_batcher* b) {
   rte_index* x = b->idx;
-  int L, k, NL, NB, wpb, grid;
+  int L, k, NL, NB, wpb, grid, team;
   size_t smem;
-  rte_status s = search_plan(x, &b->prm, b->cap, &L, &k, &NL, &NB, &wpb, &grid, &smem);
+  rte_status s = search_plan(x, &b->prm, b->cap, &L, &k, &NL, &NB, &wpb, &grid, &smem, &team);
   if (s != RTE_OK) return s;
   b->k = k;
   RTE_CUDA(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
@@ -170,6 +171,9 @@ rte_status capture(rte_batcher* b) {
     a.rerank = b->prm.rerank;
     a.n_leaves = x->has_kdtree ? (int)x->kd.n_leaves : 1;
     a.max_hits = 1;
+    // automatic teams follow the live batch size, which the graph reads on
+    // the device; the grid, planned for the capacity, leaves them room
+    a.team = b->prm.team_warps == 0 ? -team_floor(b->prm.precision, L, wpb) : team;
     e = launch_search(a, x->C, NL, NB, b->prm.precision, wpb, grid, smem, st);
   }
   cudaError_t e2 = cudaStreamEndCapture(st, &b->graph);

@@ -160,6 +160,73 @@ def test_merge_by_rank_and_network_match_oracle(lib, orc, cuda, d, R, L, W, kind
     assert np.array_equal(dd, od)
 
 
+# Teams: 2, 4 or 8 warps share each query's distance evaluations.  Every
+# distance path (tensor-core BF16, FP32 rows in registers, rows of any chunk
+# count, 960 dims, degree 16, the rerank) gives the single warp's results bit
+# for bit, and the FP32 ones the oracle's.
+TEAM_CASES = [
+    # d, integer, degree, beam, width, precision, rerank, entry mode
+    (128, True, 64, 32, 1, 0, 0, 1),
+    (128, True, 64, 16, 1, 1, 1, 1),
+    (96, False, 32, 64, 2, 0, 0, 0),
+    (160, True, 32, 64, 1, 0, 0, 1),
+    (160, False, 32, 32, 1, 1, 1, 1),
+    (960, False, 64, 32, 1, 2, 1, 1),
+    (128, True, 16, 32, 1, 0, 0, 1),
+    (64, True, 32, 256, 4, 0, 0, 1),
+]
+
+
+@pytest.mark.parametrize("d,integer,R,L,W,prec,rr,mode", TEAM_CASES)
+def test_teams_match_single_warp_and_oracle(lib, orc, cuda, d, integer, R, L, W, prec, rr, mode):
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(2500, 120, d, integer, seed=3 * d + L + W + prec)
+    graph = ds.knn_graph(base, R)
+    idx = _index(base, graph, 24, 0.2)
+    kw = dict(beam=L, k=L, search_width=W, precision=prec, rerank=rr, entry_mode=mode)
+    ids1, d1 = idx.search_projected(q, params=r.default_params(team_warps=1, **kw))
+    c1 = idx.counters(q, params=r.default_params(team_warps=1, **kw))
+    for team in (2, 4, 8):
+        p = r.default_params(team_warps=team, **kw)
+        ids, dd = idx.search_projected(q, params=p)
+        assert np.array_equal(ids, ids1) and np.array_equal(dd, d1), team
+        assert np.array_equal(idx.counters(q, params=p), c1), team
+    if prec == 0:
+        _, _, pids = idx.kdtree()
+        oids, od = orc.search(base, q, graph, L=L, k=L, search_width=W, entry_mode=mode, leaf_pids=pids,
+                              hits=idx.locate(q))
+        assert np.array_equal(ids1, oids) and np.array_equal(d1, od)
+
+
+def test_automatic_teams_on_small_batches(lib, cuda):
+    """team_warps = 0 spreads a small batch over up to 8 warps per query (and
+    a large one over one): same results as one warp per query, for batches
+    from 1 query to more than the resident warps."""
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(3000, 6000, 128, True, seed=77)
+    idx = _index(base, ds.knn_graph(base, 64), 24, 0.2)
+    for nq in (1, 37, 600, 6000):
+        for prec in (0, 1):
+            kw = dict(beam=32, k=10, precision=prec, rerank=prec)
+            a = idx.search_projected(q[:nq], params=r.default_params(team_warps=0, **kw))
+            b = idx.search_projected(q[:nq], params=r.default_params(team_warps=1, **kw))
+            assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), (nq, prec)
+
+
+def test_team_parameter_errors(lib, cuda):
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(2000, 10, 64, True, seed=5)
+    idx = _index(base, ds.knn_graph(base, 32), 24, 0.2)
+    for bad in (dict(team_warps=3), dict(team_warps=16), dict(team_warps=-1),
+                dict(team_warps=8, warps_per_block=4)):
+        with pytest.raises(r.RteError) as e:
+            idx.search_projected(q, params=r.default_params(beam=32, k=10, **bad))
+        assert "team_warps" in str(e.value)
+
+
 def test_topk_prefix_and_host_device_io(lib, orc, cuda):
     import torch
     from rt_entry_gb300 import datasets as ds

@@ -38,6 +38,22 @@ def test_batcher_equals_direct_search_for_every_batch_size(lib, cuda, prec):
     b.close()
 
 
+def test_batcher_teams_follow_the_live_batch_size(lib, cuda):
+    """The replayed search picks its team size on the device from the live
+    batch: up to 8 warps per query for a small batch, one (a team of one)
+    when the batch fills the resident warps.  Every size equals the direct
+    search."""
+    import rt_entry_gb300 as r
+    idx, base, q = _index(nq=6000, seed=43)
+    p = r.default_params(beam=32, k=10)
+    want, wd = idx.search(q, params=r.default_params(beam=32, k=10, team_warps=1))
+    b = idx.batcher(6000, params=p)
+    for s, e in [(0, 6000), (0, 100), (100, 3100), (3100, 3101)]:
+        ids, dd = b.search(q[s:e])
+        assert np.array_equal(ids, want[s:e]) and np.array_equal(dd, wd[s:e]), (s, e)
+    b.close()
+
+
 def test_learned_batcher_equals_direct_search(lib, cuda):
     """Learned entries through the CUDA graph (projection with the head's
     input, fused head, subtree location, kd-tree location on a parallel
