@@ -30,8 +30,8 @@ payloads go to stderr (and to --details FILE), not the JSON line.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--configs 1,2,3,4] [--no-stream] [--details FILE]
-  python bench.py --profile search|path [--nq N] [--beam L] [--width W]
-                  [--entry 1|2] [--precision 0|1|2] [--rerank 0|1]
+  python bench.py --profile search|path [--config 1..4] [--nq N] [--beam L]
+                  [--width W] [--entry 1|2] [--precision 0|1|2] [--rerank 0|1]
 
 --impl reference: the reference's search logic restated on the host cores
 (the oracle port, OpenMP over queries) on the config-2 workload.
@@ -587,20 +587,21 @@ def other_config(B, cfg, n4):
 
 
 def profile_mode(args):
-    """Two launches on the config-2 index for a profiler: one warm-up, one
-    to capture (inside the NVTX range `rte_profiled`).  `search`: the search
-    stage alone (rte_search_projected); `path`: the whole query call from
-    raw queries (projection, entry location, learned head, search).  Prints
-    the captured launch's event time and algorithmic bytes."""
+    """Two launches on a config's index (--config, default 2) for a
+    profiler: one warm-up, one to capture (inside the NVTX range
+    `rte_profiled`).  `search`: the search stage alone
+    (rte_search_projected); `path`: the whole query call from raw queries
+    (projection, entry location, learned head, search).  Prints the captured
+    launch's event time and algorithmic bytes."""
     import torch
     import rt_entry_gb300 as r
     from rt_entry_gb300 import build as rbuild
     from rt_entry_gb300 import datasets as ds
     rbuild.build()
-    w = ds.make_config(2, nq=args.nq, with_gt=False, device="cuda")
+    w = ds.make_config(args.config, nq=args.nq, with_gt=False, device="cuda")
     idx = r.Index.from_arrays(w.base, w.graph).build_pca().build_kdtree(LEAF, EXPAND)
     if args.entry == 2:
-        idx.train_learned(ds.training_queries(2, 200_000))
+        idx.train_learned(ds.training_queries(args.config, 200_000))
     qd = torch.from_numpy(w.queries).cuda()
     qp = idx.project(qd)
     hits = idx.locate(qp) if args.entry == 1 else idx.learned_leaves(qp)
@@ -627,7 +628,8 @@ def profile_mode(args):
     elem = {0: 4, 1: 2, 2: 1}[args.precision]
     alg = algorithmic_bytes(cnt, w.base.shape[1], args.beam, w.graph.shape[1], K_TOP, elem,
                             args.precision != 0 and args.rerank == 1, 4 if args.precision == 2 else 0)
-    print(json.dumps({"mode": args.profile, "nq": args.nq, "precision": args.precision, "beam": args.beam,
+    print(json.dumps({"mode": args.profile, "config": args.config, "nq": args.nq, "precision": args.precision,
+                      "beam": args.beam,
                       "width": args.width, "entry": args.entry, "ms": ms, "alg_bytes": alg,
                       "alg_gbs": alg / ms / 1e6, "mean_dist_evals": float(cnt[:, 2].mean()),
                       "mean_expanded": float(cnt[:, 1].mean())}), flush=True)
@@ -651,6 +653,7 @@ def main():
     ap.add_argument("--entry", type=int, default=1, help="--profile: 1 kd-tree, 2 learned")
     ap.add_argument("--precision", type=int, default=0, help="--profile: 0 FP32, 1 BF16, 2 FP8")
     ap.add_argument("--rerank", type=int, default=0, help="--profile: exact FP32 rerank")
+    ap.add_argument("--config", type=int, default=2, choices=(1, 2, 3, 4), help="--profile: workload")
     args = ap.parse_args()
     if args.profile:
         profile_mode(args)

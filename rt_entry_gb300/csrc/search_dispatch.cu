@@ -16,16 +16,19 @@ void* search_lookup_c30_f32(int, int, bool, bool);
 void* search_lookup_c30_fp8(int, int, bool, bool);
 void* search_lookup_c3_bf16(int, int, bool, bool);
 void* search_lookup_c3_bf16_r16(int, int, bool, bool);
+void* search_lookup_c3_bf16_wide(int, int, bool, bool);
 void* search_lookup_c3_f32(int, int, bool, bool);
 void* search_lookup_c3_f32_r16(int, int, bool, bool);
 void* search_lookup_c3_fp8(int, int, bool, bool);
 void* search_lookup_c3_fp8_r16(int, int, bool, bool);
+void* search_lookup_c3_fp8_wide(int, int, bool, bool);
 void* search_lookup_c4_bf16(int, int, bool, bool);
 void* search_lookup_c4_bf16_r16(int, int, bool, bool);
 void* search_lookup_c4_f32(int, int, bool, bool);
 void* search_lookup_c4_f32_r16(int, int, bool, bool);
 void* search_lookup_c4_fp8(int, int, bool, bool);
 void* search_lookup_c4_fp8_r16(int, int, bool, bool);
+void* search_lookup_c4_fp8_wide(int, int, bool, bool);
 void* search_lookup_cg_bf16(int, int, bool, bool);
 void* search_lookup_cg_bf16_wide(int, int, bool, bool);
 void* search_lookup_cg_bf16_r16(int, int, bool, bool);
@@ -54,11 +57,11 @@ const Entry kTable[] = {
     {1, chain<search_lookup_c1_f32, search_lookup_c1_f32_r16>, nullptr, nullptr},
     {2, chain<search_lookup_c2_f32, search_lookup_c2_f32_r16>, nullptr, nullptr},
     {3, chain<search_lookup_c3_f32, search_lookup_c3_f32_r16>,
-     chain<search_lookup_c3_bf16, search_lookup_c3_bf16_r16>,
-     chain<search_lookup_c3_fp8, search_lookup_c3_fp8_r16>},
+     chain<search_lookup_c3_bf16, search_lookup_c3_bf16_wide, search_lookup_c3_bf16_r16>,
+     chain<search_lookup_c3_fp8, search_lookup_c3_fp8_wide, search_lookup_c3_fp8_r16>},
     {4, chain<search_lookup_c4_f32, search_lookup_c4_f32_r16>,
      chain<search_lookup_c4_bf16, search_lookup_c4_bf16_r16>,
-     chain<search_lookup_c4_fp8, search_lookup_c4_fp8_r16>},
+     chain<search_lookup_c4_fp8, search_lookup_c4_fp8_wide, search_lookup_c4_fp8_r16>},
     {30, search_lookup_c30_f32, search_lookup_c30_bf16, search_lookup_c30_fp8},
 };
 // Kernels for any chunk count (template C == 0): every other dimension up

@@ -464,32 +464,39 @@ __device__ __forceinline__ void make_query_extra(QueryExtra<C, kPrecBF16, true>&
   __syncwarp();
 }
 
-// Requests every valid row's 128-byte lines into L2 (lines spread over the
-// lanes), so the gathers below find their rows in flight or in L2.
-template <int kRowBytes>
-__device__ __forceinline__ void prefetch_rows(const char* rows, const int* s_ids, int n, int lane) {
-  constexpr int kLines = (kRowBytes + 127) / 128;
-  for (int i = lane; i < n * kLines; i += 32) {
-    const int row = i / kLines, line = i - row * kLines;
-    const char* p = rows + (size_t)s_ids[row] * kRowBytes + line * 128;
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-  }
+// L2 prefetch of the rows a warp is about to gather.  A batch of up to
+// kPrefetchWhole bytes is prefetched at once.  A larger one goes through a
+// window of about kPrefetchBytes per warp: the first `ahead` rows of the
+// warp's share before its first group, then at each group the rows `ahead`
+// further on.  Without the window a batch of 256 rows of 3.8 KB would put
+// ~1 MB per warp in flight, several GB over the grid against a 129 MB L2,
+// and the lines would be evicted before use (on one GB300: 1.7x the
+// algorithmic bytes read from DRAM).  Batches of up to 128 KB (256 FP32
+// rows of 128 dims) measured faster prefetched whole.
+constexpr int kPrefetchBytes = 16384;
+constexpr int kPrefetchWhole = 196608;
+
+__host__ __device__ constexpr int prefetch_ahead(int row_bytes, int G) {
+  return kPrefetchBytes / row_bytes >= G ? kPrefetchBytes / row_bytes / G * G : G;
+}
+// Rows to prefetch before the first group: all n, or the window.
+__device__ __forceinline__ int prefetch_first(int n, int row_bytes, int ahead) {
+  return n * row_bytes <= kPrefetchWhole ? n : ahead;
 }
 
-// The same for the rows of a team member's share: groups of G rows, group
-// g belonging to member g % K.  lines = 128-byte lines per row.
+// Prefetches rows [lr0, lr1) of member w's share of a K-warp team (groups
+// of G rows, group g belonging to member g % K; a single warp is w = 0,
+// K = 1), `lines` 128-byte lines per row.
 template <int G>
-__device__ __forceinline__ void prefetch_share(const char* rows, size_t row_bytes, int lines,
-                                               const int* s_ids, int n, int lane, int w, int K) {
-  const int per = G * lines;
-  for (int i = lane;; i += 32) {
-    const int j = i / per;
-    const int g0 = G * (w + j * K);
-    if (g0 >= n) break;
-    const int r = i - j * per;
-    const int row = g0 + r / lines;
-    if (row < n)
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(rows + (size_t)s_ids[row] * row_bytes + (r % lines) * 128));
+__device__ __forceinline__ void prefetch_local(const char* rows, size_t row_bytes, int lines,
+                                               const int* s_ids, int n, int lane, int w, int K, int lr0,
+                                               int lr1) {
+  for (int i = lane + lr0 * lines; i < lr1 * lines; i += 32) {
+    const int lr = i / lines, line = i - lr * lines;
+    const int j = lr / G;
+    const int row = G * (w + j * K) + (lr - j * G);
+    if (row >= n) break;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(rows + (size_t)s_ids[row] * row_bytes + line * 128));
   }
 }
 
@@ -500,15 +507,18 @@ __device__ __forceinline__ void prefetch_share(const char* rows, size_t row_byte
 template <int C, bool TEAM>
 __device__ __forceinline__ void distances_mma(const SearchArgs& a, const QueryExtra<C, kPrecBF16, true>& qx,
                                               const int* s_ids, float* s_dist, int n, int lane, int w, int K) {
-  constexpr int kRowBytes = 64 * C;
+  constexpr int kRowBytes = 64 * C, kLines = (kRowBytes + 127) / 128;
+  constexpr int kAhead = prefetch_ahead(kRowBytes, 8);
   const char* rows = reinterpret_cast<const char*>(a.base_bf16);
-  if constexpr (TEAM)
-    prefetch_share<8>(rows, kRowBytes, (kRowBytes + 127) / 128, s_ids, n, lane, w, K);
-  else
-    prefetch_rows<kRowBytes>(rows, s_ids, n, lane);
+  const int ws = TEAM ? w : 0, ks = TEAM ? K : 1;
+  const int first_rows = prefetch_first(n, kRowBytes, kAhead);
+  prefetch_local<8>(rows, kRowBytes, kLines, s_ids, n, lane, ws, ks, 0, first_rows);
+  const bool windowed = first_rows < n;
   const int g = lane >> 2, t = lane & 3;
-  const int first = TEAM ? 8 * w : 0, step = TEAM ? 8 * K : 8;
-  for (int r0 = first; r0 < n; r0 += step) {
+  const int first = 8 * ws, step = 8 * ks;
+  int j = 0;
+  for (int r0 = first; r0 < n; r0 += step, ++j) {
+    if (windowed) prefetch_local<8>(rows, kRowBytes, kLines, s_ids, n, lane, ws, ks, kAhead + 8 * j, kAhead + 8 * j + 8);
     const int ra = r0 + g;
     const int id = s_ids[ra < n ? ra : r0];
     const char* p = rows + (size_t)id * kRowBytes + 16 * t;
@@ -643,23 +653,20 @@ __device__ __forceinline__ void distances_rt(const SearchArgs& a, const float* q
   constexpr int G = 4;
   const int C = a.C, n4 = C >> 2, rem = C & 3;
   const size_t stride = 32 * (size_t)C;  // elements per row
-  {
-    const int lines = (int)((stride * SlabLoader<PREC>::kBytes + 127) / 128);
-    const char* rows = PREC == kPrecF32    ? reinterpret_cast<const char*>(a.base)
-                       : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
-                                           : reinterpret_cast<const char*>(a.base_fp8);
-    const size_t rb = stride * SlabLoader<PREC>::kBytes;
-    if constexpr (TEAM) {
-      prefetch_share<G>(rows, rb, lines, s_ids, n, lane, w, K);
-    } else {
-      for (int i = lane; i < n * lines; i += 32) {
-        const int row = i / lines, line = i - row * lines;
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(rows + (size_t)s_ids[row] * rb + line * 128));
-      }
-    }
-  }
-  const int first = TEAM ? G * w : 0, step = TEAM ? G * K : G;
-  for (int g0 = first; g0 < n; g0 += step) {
+  const int lines = (int)((stride * SlabLoader<PREC>::kBytes + 127) / 128);
+  const char* rows = PREC == kPrecF32    ? reinterpret_cast<const char*>(a.base)
+                     : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
+                                         : reinterpret_cast<const char*>(a.base_fp8);
+  const size_t rb = stride * SlabLoader<PREC>::kBytes;
+  const int ws = TEAM ? w : 0, ks = TEAM ? K : 1;
+  const int ahead = prefetch_ahead((int)rb, G);
+  const int first_rows = prefetch_first(n, (int)rb, ahead);
+  prefetch_local<G>(rows, rb, lines, s_ids, n, lane, ws, ks, 0, first_rows);
+  const bool windowed = first_rows < n;
+  const int first = G * ws, step = G * ks;
+  int j = 0;
+  for (int g0 = first; g0 < n; g0 += step, ++j) {
+    if (windowed) prefetch_local<G>(rows, rb, lines, s_ids, n, lane, ws, ks, ahead + G * j, ahead + G * j + G);
     SlabLoader<PREC> r[G];
 #pragma unroll
     for (int t = 0; t < G; ++t) r[t].init(a, s_ids[g0 + t < n ? g0 + t : g0], stride);
@@ -721,18 +728,16 @@ __device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)
     distances_mma<C, TEAM>(a, qx, s_ids, s_dist, n, lane, w, K);
   } else {
     constexpr int G = C <= 4 ? 8 : 2;
-    {
-      constexpr int kRowBytes = 32 * C * (PREC == kPrecF32 ? 4 : PREC == kPrecBF16 ? 2 : 1);
-      const char* rows = PREC == kPrecF32    ? reinterpret_cast<const char*>(a.base)
-                         : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
-                                             : reinterpret_cast<const char*>(a.base_fp8);
-      if constexpr (TEAM)
-        prefetch_share<G>(rows, kRowBytes, (kRowBytes + 127) / 128, s_ids, n, lane, w, K);
-      else
-        prefetch_rows<kRowBytes>(rows, s_ids, n, lane);
-    }
-    const int first = TEAM ? G * w : 0, step = TEAM ? G * K : G;
-    for (int g0 = first; g0 < n; g0 += step) {
+    constexpr int kRowBytes = 32 * C * (PREC == kPrecF32 ? 4 : PREC == kPrecBF16 ? 2 : 1);
+    constexpr int kLines = (kRowBytes + 127) / 128, kAhead = prefetch_ahead(kRowBytes, G);
+    const char* rows = PREC == kPrecF32    ? reinterpret_cast<const char*>(a.base)
+                       : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
+                                           : reinterpret_cast<const char*>(a.base_fp8);
+    const int ws = TEAM ? w : 0, ks = TEAM ? K : 1;
+    const int first_rows = prefetch_first(n, kRowBytes, kAhead);
+    prefetch_local<G>(rows, kRowBytes, kLines, s_ids, n, lane, ws, ks, 0, first_rows);
+    const int first = G * ws, step = G * ks;
+    auto group = [&](int g0) {
       // all G loads first, unconditionally (a short group re-reads its first
       // row), so they are issued back to back before any use
       RowLoader<C, PREC> r[G];
@@ -742,6 +747,17 @@ __device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)
 #pragma unroll
       for (int t = 0; t < G; ++t) part[t] = g0 + t < n ? lane_partial<C>(r[t].v, qv) : 0.0f;
       reduce_rows<G>(part, s_dist, g0, n, lane);
+    };
+    // the window's loop is a copy of its own: the whole-batch loop keeps no
+    // window state in the registers these rows fill
+    if (first_rows >= n) {
+      for (int g0 = first; g0 < n; g0 += step) group(g0);
+    } else {
+      int j = 0;
+      for (int g0 = first; g0 < n; g0 += step, ++j) {
+        prefetch_local<G>(rows, kRowBytes, kLines, s_ids, n, lane, ws, ks, kAhead + G * j, kAhead + G * j + G);
+        group(g0);
+      }
     }
   }
 }
@@ -1179,8 +1195,18 @@ __device__ __forceinline__ void help_query(const SearchArgs& a, int q, int lane,
   }
 }
 
+// Blocks of 8 warps per SM the register budget is set for: 4 (64 registers
+// a thread), or 2 (128) for rows of more than 4 chunks in registers and for
+// the kernels built for any chunk count with a pool or batch of 8
+// registers.  Those spilled over 1 KB at 64 registers; at 128 the 960-d
+// search with 256-slot pools and batches ran 1.5x faster on one GB300,
+// while the specialised 96- and 128-d kernels of the same pool ran slower.
+__host__ __device__ constexpr int search_min_blocks(int C, int NL, int NB) {
+  return C > 4 || (C == 0 && (NL >= 8 || NB >= 8)) ? 2 : 4;
+}
+
 template <int C, int NL, int NB, int PREC, bool R16 = false>
-__global__ void __launch_bounds__(256, (C <= 4 ? 4 : 2)) search_kernel(SearchArgs a) {
+__global__ void __launch_bounds__(256, search_min_blocks(C, NL, NB)) search_kernel(SearchArgs a) {
   extern __shared__ uint32_t smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -1216,7 +1242,7 @@ __global__ void __launch_bounds__(256, (C <= 4 ? 4 : 2)) search_kernel(SearchArg
 // are; a team never spans blocks (the launch keeps warps per block a
 // multiple of K, and K falls back to 1 otherwise).
 template <int C, int NL, int NB, int PREC, bool R16 = false>
-__global__ void __launch_bounds__(256, (C <= 4 ? 4 : 2)) search_kernel_team(SearchArgs a) {
+__global__ void __launch_bounds__(256, search_min_blocks(C, NL, NB)) search_kernel_team(SearchArgs a) {
   extern __shared__ uint32_t smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;

@@ -395,6 +395,26 @@ def test_low_precision_paths_match_oracle(lib, orc, cuda, prec, rerank, L):
     assert np.array_equal(dd, od)
 
 
+@pytest.mark.parametrize("d,R,L,W", [(96, 32, 128, 4), (96, 32, 256, 4), (128, 64, 64, 2), (128, 64, 256, 4)])
+@pytest.mark.parametrize("prec", [1, 2])
+def test_low_precision_wide_batches_match_oracle(lib, orc, cuda, d, R, L, W, prec):
+    """Batches of 4 and 8 registers (width 4 over degree 32, widths 2 and 4
+    over degree 64) on the tensor-core BF16 and the FP8 kernels, with the
+    FP32 rerank: integer data, bit-exact with the oracle."""
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(3000, 150, d, True, seed=d + R + L + W + prec)
+    graph = ds.knn_graph(base, R)
+    idx = _index(base, graph, 32, 0.2)
+    _, _, pids = idx.kdtree()
+    hits = idx.locate(q)
+    low = idx.search_base_lowp(prec)
+    ids, dd = idx.search_projected(q, beam=L, k=L, search_width=W, precision=prec, rerank=1)
+    oids, od = orc.search(low, q, graph, L=L, k=L, search_width=W, leaf_pids=pids, hits=hits,
+                          rerank_base=base)
+    assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
+    assert np.array_equal(dd, od)
+
+
 @pytest.mark.parametrize("L,W", [(16, 1), (64, 1), (32, 4)])
 @pytest.mark.parametrize("prec", [1, 2])
 def test_low_precision_paths_on_degree16_graph_match_oracle(lib, orc, cuda, prec, L, W):
