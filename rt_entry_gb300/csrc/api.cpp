@@ -268,12 +268,12 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
     if (team > 1 && pl.wpb % team != 0)
       return fail(RTE_EINVAL, "warps_per_block must be a multiple of team_warps");
   } else {
-    pl.wpb = (int)std::min<size_t>(8, smem_cap / per_warp);
+    pl.wpb = (int)std::min<size_t>(8, (smem_cap - kBlockShareBytes) / per_warp);
     if (team > 1) pl.wpb -= pl.wpb % team;  // whole teams per block
     if (team > 1 && pl.wpb < team)
       return fail(RTE_EINVAL, "the bloom filter leaves room for fewer warps per block than team_warps");
   }
-  pl.smem = (size_t)pl.wpb * per_warp;
+  pl.smem = (size_t)pl.wpb * per_warp + kBlockShareBytes;
   if (pl.wpb < 1 || pl.smem > smem_cap)
     return fail(RTE_EINVAL, "bloom filter too large for the block's shared memory");
   const int occ = occupancy_search(x->C, pl.NL, pl.NB, pl.prec, r16, pl.wpb, pl.smem);
@@ -317,9 +317,12 @@ cudaError_t side_stream(int dev, SideStream** out) {
 }
 
 // Projection + locate + search on device buffers.
+// host_err (pinned), when given, receives in stream order the call's error
+// word: a bounded device wait ran out when it is non-zero.
 rte_status run_query_path(rte_index* x, const float* d_queries, bool already_projected,
                           const int32_t* d_hits_in, int64_t nq, const rte_search_params* prm,
-                          int32_t* d_ids, float* d_dists, long long* d_counters, cudaStream_t st) {
+                          int32_t* d_ids, float* d_dists, long long* d_counters, cudaStream_t st,
+                          int* host_err = nullptr) {
   Plan pl;
   rte_status s = plan_search(x, prm, nq, pl);
   if (s != RTE_OK) return s;
@@ -423,10 +426,11 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
     }
     if (ls != RTE_OK) return ls;
   }
-  if (!zwork) {
-    RTE_CUDA(work.alloc(4, st));
-    RTE_CUDA(cudaMemsetAsync(work.p, 0, 4, st));
+  if (!zwork) {  // the work counter and an error word
+    RTE_CUDA(work.alloc(8, st));
+    RTE_CUDA(cudaMemsetAsync(work.p, 0, 8, st));
   }
+  int* err_word = zwork ? zerr : work.as<int>() + 1;
   AsyncBuf poolb;
   if (full_rerank) RTE_CUDA(poolb.alloc((size_t)nq * pl.L * 4, st));
   SearchArgs a{};
@@ -460,7 +464,9 @@ rte_status run_query_path(rte_index* x, const float* d_queries, bool already_pro
   a.n_leaves = x->has_kdtree ? (int)x->kd.n_leaves : 1;
   a.max_hits = prm->max_hits;
   a.team = pl.team;
+  a.err = err_word;
   RTE_CUDA(launch_search(a, x->C, pl.NL, pl.NB, pl.prec, pl.wpb, pl.grid, pl.smem, st));
+  if (host_err) RTE_CUDA(cudaMemcpyAsync(host_err, err_word, sizeof(int), cudaMemcpyDeviceToHost, st));
   if (full_rerank)
     RTE_CUDA(launch_rerank_full(x->raw.p, x->np, x->dim, d_queries, x->dim, poolb.as<int32_t>(),
                                 (int)nq, pl.L, pl.k, d_ids, d_dists, x->num_sms, st));
@@ -923,12 +929,20 @@ static rte_status search_common(rte_index* x, const float* q, bool projected, co
       dc = reinterpret_cast<long long*>(counters);
     }
   }
-  s = run_query_path(x, dq, projected, dh, nq, prm, di, dd, dc, st);
+  const bool syncs = host_io || ids_host || dists_host || cnt_host;
+  // the error word comes back to pinned memory, so its copy stays in stream order
+  thread_local int* herr = nullptr;
+  if (syncs && !herr) RTE_CUDA(cudaMallocHost(&herr, sizeof(int)));
+  if (syncs) *herr = 0;
+  s = run_query_path(x, dq, projected, dh, nq, prm, di, dd, dc, st, syncs ? herr : nullptr);
   if (s != RTE_OK) return s;
   if (ids_host) RTE_CUDA(cudaMemcpyAsync(out_ids, di, obytes, cudaMemcpyDeviceToHost, st));
   if (dists_host) RTE_CUDA(cudaMemcpyAsync(out_dists, dd, obytes, cudaMemcpyDeviceToHost, st));
   if (cnt_host) RTE_CUDA(cudaMemcpyAsync(counters, dc, (size_t)nq * 32, cudaMemcpyDeviceToHost, st));
-  if (host_io || ids_host || dists_host || cnt_host) RTE_CUDA(cudaStreamSynchronize(st));
+  if (syncs) {
+    RTE_CUDA(cudaStreamSynchronize(st));
+    if (*herr) return fail(RTE_ETIMEOUT, "a bounded wait in the query path ran out (code " + std::to_string(*herr) + ")");
+  }
   return RTE_OK;
 }
 

@@ -33,7 +33,8 @@ namespace {
 // Largest batch one call accepts (RTE_NOALLOC_MAX_QUERIES in rtentry.h).
 constexpr int kMaxQueries = 65536;
 
-// [0, 256): the search's work counter (first 4 bytes); [256, ...): hits.
+// [0, 256): the search's work counter (first 4 bytes) and its error word
+// (next 4: a bounded wait ran out); [256, ...): hits.
 struct NoallocScratch {
   unsigned int counter[64];
   int32_t hits[kMaxQueries];
@@ -118,8 +119,9 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
     RTE_CUDA(launch_locate(x->d_wide.p, (int)x->d_wide.n, projected, nq, x->search_dim, scr->hits, st));
     h = scr->hits;
   }
-  // the array keeps the previous call's contents: the counter must restart at 0
-  RTE_CUDA(cudaMemsetAsync(scr->counter, 0, sizeof(unsigned int), st));
+  // the array keeps the previous call's contents: the counter and the error
+  // word must restart at 0
+  RTE_CUDA(cudaMemsetAsync(scr->counter, 0, 2 * sizeof(unsigned int), st));
   SearchArgs a{};
   a.base = x->il32.p;
   a.base_bf16 = x->il16.p;
@@ -135,6 +137,7 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   a.out_dists = out_dists;
   a.counters = nullptr;
   a.work = scr->counter;
+  a.err = reinterpret_cast<int*>(scr->counter + 1);
   a.np = (int)x->np;
   a.d = x->search_dim;
   a.qstride = x->search_dim;

@@ -504,6 +504,42 @@ __device__ __forceinline__ void prefetch_local(const char* rows, size_t row_byte
 // group: thread (g, t) supplies row g of the group as column g of the MMA's
 // B operand; the query is every row of A, so D[.][col] is the dot product of
 // row col, and lanes 0..3 hold the group's eight results.
+// One group of 8 rows from r0 (rows >= n are skipped).
+template <int C>
+__device__ __forceinline__ void mma_group(const SearchArgs& a, const QueryExtra<C, kPrecBF16, true>& qx,
+                                          const int* s_ids, float* s_dist, int n, int lane, int r0) {
+  constexpr int kRowBytes = 64 * C;
+  const char* rows = reinterpret_cast<const char*>(a.base_bf16);
+  const int g = lane >> 2, t = lane & 3;
+  const int ra = r0 + g;
+  const int id = s_ids[ra < n ? ra : r0];
+  const char* p = rows + (size_t)id * kRowBytes + 16 * t;
+  uint4 v[C];
+#pragma unroll
+  for (int i = 0; i < C; ++i) v[i] = __ldg(reinterpret_cast<const uint4*>(p + 64 * i));
+  // the norms of this lane's two output rows, loaded while the MMAs run
+  float pn[2] = {0.0f, 0.0f};
+  if (g == 0) {
+#pragma unroll
+    for (int e = 0; e < 2; ++e)
+      if (r0 + 2 * t + e < n) pn[e] = __ldg(a.norm16 + s_ids[r0 + 2 * t + e]);
+  }
+  float d[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int i = 0; i < C; ++i) {
+    const uint4 q = *reinterpret_cast<const uint4*>(qx.qs + 4 * t + 16 * i);
+    mma_bf16_16816(d, q.x, q.x, q.y, q.y, v[i].x, v[i].y);
+    mma_bf16_16816(d, q.z, q.z, q.w, q.w, v[i].z, v[i].w);
+  }
+  if (g == 0) {
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int row = r0 + 2 * t + e;
+      if (row < n) s_dist[row] = __fmaf_rn(-2.0f, d[e], __fadd_rn(pn[e], qx.qn));
+    }
+  }
+}
+
 template <int C, bool TEAM>
 __device__ __forceinline__ void distances_mma(const SearchArgs& a, const QueryExtra<C, kPrecBF16, true>& qx,
                                               const int* s_ids, float* s_dist, int n, int lane, int w, int K) {
@@ -514,38 +550,11 @@ __device__ __forceinline__ void distances_mma(const SearchArgs& a, const QueryEx
   const int first_rows = prefetch_first(n, kRowBytes, kAhead);
   prefetch_local<8>(rows, kRowBytes, kLines, s_ids, n, lane, ws, ks, 0, first_rows);
   const bool windowed = first_rows < n;
-  const int g = lane >> 2, t = lane & 3;
   const int first = 8 * ws, step = 8 * ks;
   int j = 0;
   for (int r0 = first; r0 < n; r0 += step, ++j) {
     if (windowed) prefetch_local<8>(rows, kRowBytes, kLines, s_ids, n, lane, ws, ks, kAhead + 8 * j, kAhead + 8 * j + 8);
-    const int ra = r0 + g;
-    const int id = s_ids[ra < n ? ra : r0];
-    const char* p = rows + (size_t)id * kRowBytes + 16 * t;
-    uint4 v[C];
-#pragma unroll
-    for (int i = 0; i < C; ++i) v[i] = __ldg(reinterpret_cast<const uint4*>(p + 64 * i));
-    // the norms of this lane's two output rows, loaded while the MMAs run
-    float pn[2] = {0.0f, 0.0f};
-    if (g == 0) {
-#pragma unroll
-      for (int e = 0; e < 2; ++e)
-        if (r0 + 2 * t + e < n) pn[e] = __ldg(a.norm16 + s_ids[r0 + 2 * t + e]);
-    }
-    float d[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-    for (int i = 0; i < C; ++i) {
-      const uint4 q = *reinterpret_cast<const uint4*>(qx.qs + 4 * t + 16 * i);
-      mma_bf16_16816(d, q.x, q.x, q.y, q.y, v[i].x, v[i].y);
-      mma_bf16_16816(d, q.z, q.z, q.w, q.w, v[i].z, v[i].w);
-    }
-    if (g == 0) {
-#pragma unroll
-      for (int e = 0; e < 2; ++e) {
-        const int row = r0 + 2 * t + e;
-        if (row < n) s_dist[row] = __fmaf_rn(-2.0f, d[e], __fadd_rn(pn[e], qx.qn));
-      }
-    }
+    mma_group<C>(a, qx, s_ids, s_dist, n, lane, r0);
   }
 }
 
@@ -647,17 +656,74 @@ __device__ __forceinline__ void reduce_rows(float (&part)[G], float* s_dist, int
 
 // Distances of n rows of a.C chunks against the query row in shared memory
 // qs (interleaved layout), G rows in flight.
+// One group of 4 rows from g0 of a run-time chunk count (rows >= n give 0).
+template <int PREC>
+__device__ __forceinline__ void rt_group(const SearchArgs& a, const float* qs, const int* s_ids,
+                                         float* s_dist, int n, int lane, int g0) {
+  constexpr int G = 4;
+  const int C = a.C, n4 = C >> 2, rem = C & 3;
+  const size_t stride = 32 * (size_t)C;  // elements per row
+  SlabLoader<PREC> r[G];
+#pragma unroll
+  for (int t = 0; t < G; ++t) r[t].init(a, s_ids[g0 + t < n ? g0 + t : g0], stride);
+  float part[G];
+#pragma unroll
+  for (int t = 0; t < G; ++t) part[t] = 0.0f;
+#pragma unroll 2
+  for (int sl = 0; sl < n4; ++sl) {
+    const float4 q = *reinterpret_cast<const float4*>(qs + 128 * sl + 4 * lane);
+    float4 v[G];
+#pragma unroll
+    for (int t = 0; t < G; ++t) v[t] = r[t].quad(128 * sl, lane);
+#pragma unroll
+    for (int t = 0; t < G; ++t) {
+      part[t] = chunk_acc(v[t].x, q.x, part[t]);
+      part[t] = chunk_acc(v[t].y, q.y, part[t]);
+      part[t] = chunk_acc(v[t].z, q.z, part[t]);
+      part[t] = chunk_acc(v[t].w, q.w, part[t]);
+    }
+  }
+  int off = 128 * n4;
+  if (rem >= 2) {
+    const float2 q = *reinterpret_cast<const float2*>(qs + off + 2 * lane);
+#pragma unroll
+    for (int t = 0; t < G; ++t) {
+      const float2 v = r[t].pair(off, lane);
+      part[t] = chunk_acc(v.x, q.x, part[t]);
+      part[t] = chunk_acc(v.y, q.y, part[t]);
+    }
+    off += 64;
+  }
+  if (rem & 1) {
+    const float q = qs[off + lane];
+#pragma unroll
+    for (int t = 0; t < G; ++t) part[t] = chunk_acc(r[t].one(off, lane), q, part[t]);
+  }
+#pragma unroll
+  for (int t = 0; t < G; ++t)
+    if (g0 + t >= n) part[t] = 0.0f;
+  reduce_rows<G>(part, s_dist, g0, n, lane);
+}
+
+template <int PREC>
+__host__ __device__ constexpr int slab_bytes() {
+  return PREC == kPrecF32 ? 4 : PREC == kPrecBF16 ? 2 : 1;
+}
+
+template <int PREC>
+__device__ __forceinline__ const char* search_rows(const SearchArgs& a) {
+  return PREC == kPrecF32    ? reinterpret_cast<const char*>(a.base)
+         : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
+                             : reinterpret_cast<const char*>(a.base_fp8);
+}
+
 template <int PREC, bool TEAM>
 __device__ __forceinline__ void distances_rt(const SearchArgs& a, const float* qs, const int* s_ids,
                                              float* s_dist, int n, int lane, int w, int K) {
   constexpr int G = 4;
-  const int C = a.C, n4 = C >> 2, rem = C & 3;
-  const size_t stride = 32 * (size_t)C;  // elements per row
-  const int lines = (int)((stride * SlabLoader<PREC>::kBytes + 127) / 128);
-  const char* rows = PREC == kPrecF32    ? reinterpret_cast<const char*>(a.base)
-                     : PREC == kPrecBF16 ? reinterpret_cast<const char*>(a.base_bf16)
-                                         : reinterpret_cast<const char*>(a.base_fp8);
-  const size_t rb = stride * SlabLoader<PREC>::kBytes;
+  const size_t rb = 32 * (size_t)a.C * slab_bytes<PREC>();
+  const int lines = (int)((rb + 127) / 128);
+  const char* rows = search_rows<PREC>(a);
   const int ws = TEAM ? w : 0, ks = TEAM ? K : 1;
   const int ahead = prefetch_ahead((int)rb, G);
   const int first_rows = prefetch_first(n, (int)rb, ahead);
@@ -667,46 +733,7 @@ __device__ __forceinline__ void distances_rt(const SearchArgs& a, const float* q
   int j = 0;
   for (int g0 = first; g0 < n; g0 += step, ++j) {
     if (windowed) prefetch_local<G>(rows, rb, lines, s_ids, n, lane, ws, ks, ahead + G * j, ahead + G * j + G);
-    SlabLoader<PREC> r[G];
-#pragma unroll
-    for (int t = 0; t < G; ++t) r[t].init(a, s_ids[g0 + t < n ? g0 + t : g0], stride);
-    float part[G];
-#pragma unroll
-    for (int t = 0; t < G; ++t) part[t] = 0.0f;
-#pragma unroll 2
-    for (int sl = 0; sl < n4; ++sl) {
-      const float4 q = *reinterpret_cast<const float4*>(qs + 128 * sl + 4 * lane);
-      float4 v[G];
-#pragma unroll
-      for (int t = 0; t < G; ++t) v[t] = r[t].quad(128 * sl, lane);
-#pragma unroll
-      for (int t = 0; t < G; ++t) {
-        part[t] = chunk_acc(v[t].x, q.x, part[t]);
-        part[t] = chunk_acc(v[t].y, q.y, part[t]);
-        part[t] = chunk_acc(v[t].z, q.z, part[t]);
-        part[t] = chunk_acc(v[t].w, q.w, part[t]);
-      }
-    }
-    int off = 128 * n4;
-    if (rem >= 2) {
-      const float2 q = *reinterpret_cast<const float2*>(qs + off + 2 * lane);
-#pragma unroll
-      for (int t = 0; t < G; ++t) {
-        const float2 v = r[t].pair(off, lane);
-        part[t] = chunk_acc(v.x, q.x, part[t]);
-        part[t] = chunk_acc(v.y, q.y, part[t]);
-      }
-      off += 64;
-    }
-    if (rem & 1) {
-      const float q = qs[off + lane];
-#pragma unroll
-      for (int t = 0; t < G; ++t) part[t] = chunk_acc(r[t].one(off, lane), q, part[t]);
-    }
-#pragma unroll
-    for (int t = 0; t < G; ++t)
-      if (g0 + t >= n) part[t] = 0.0f;
-    reduce_rows<G>(part, s_dist, g0, n, lane);
+    rt_group<PREC>(a, qs, s_ids, s_dist, n, lane, g0);
   }
 }
 
@@ -718,6 +745,140 @@ __device__ __forceinline__ void distances_rt(const SearchArgs& a, const float* q
 // Every addition pairs the same two partial sums as the reference's
 // shuffle-down tree (addition is commutative, so the results are equal).
 // With TEAM, the groups of rows of member w of a K-warp team only.
+// Rows per distance group of each path.
+template <int C, int PREC>
+__host__ __device__ constexpr int distance_group_size() {
+  return C == 0 ? 4 : (PREC == kPrecBF16 && C <= 4) ? 8 : C <= 4 ? 8 : 2;
+}
+
+// One group of rows with the query in registers (C > 0, scalar path): all
+// G loads first, unconditionally (a short group re-reads its first row), so
+// they are issued back to back before any use.
+template <int C, int PREC>
+__device__ __forceinline__ void regs_group(const SearchArgs& a, const float (&qv)[qregs(C)], const int* s_ids,
+                                           float* s_dist, int n, int lane, int g0) {
+  constexpr int G = distance_group_size<C, PREC>();
+  RowLoader<C, PREC> r[G];
+#pragma unroll
+  for (int t = 0; t < G; ++t) r[t].load(a, s_ids[g0 + t < n ? g0 + t : g0], lane);
+  float part[G];
+#pragma unroll
+  for (int t = 0; t < G; ++t) part[t] = g0 + t < n ? lane_partial<C>(r[t].v, qv) : 0.0f;
+  reduce_rows<G>(part, s_dist, g0, n, lane);
+}
+
+// Group `grp` (rows grp*G ..) of a batch, on whichever path the kernel uses.
+template <int C, int PREC>
+__device__ __forceinline__ void distance_group(const SearchArgs& a, const float (&qv)[qregs(C)],
+                                               const QueryExtra<C, PREC>& qx, const int* s_ids,
+                                               float* s_dist, int n, int lane, int grp) {
+  constexpr int G = distance_group_size<C, PREC>();
+  if constexpr (C == 0)
+    rt_group<PREC>(a, qx.qs, s_ids, s_dist, n, lane, G * grp);
+  else if constexpr (PREC == kPrecBF16 && C <= 4)
+    mma_group<C>(a, qx, s_ids, s_dist, n, lane, G * grp);
+  else
+    regs_group<C, PREC>(a, qv, s_ids, s_dist, n, lane, G * grp);
+}
+
+// The L2 prefetch a batch's distances start with (the whole batch, or the
+// first window of a large one), for a warp that computes any of its groups.
+template <int C, int PREC>
+__device__ __forceinline__ void prefetch_batch(const SearchArgs& a, const int* s_ids, int n, int lane) {
+  constexpr int G = distance_group_size<C, PREC>();
+  const int rb = 32 * (C == 0 ? a.C : C) * slab_bytes<PREC>();
+  const int lines = (rb + 127) / 128;
+  prefetch_local<G>(search_rows<PREC>(a), rb, lines, s_ids, n, lane, 0, 1, 0,
+                    prefetch_first(n, rb, prefetch_ahead(rb, G)));
+}
+
+// ---- helping in the tail ----
+// When the query counter runs out, the warps left without a query help the
+// warps of their block still searching: a leader with idle warps in its
+// block publishes each batch's distance phase, and leader and helpers take
+// its groups of rows from one ticket.  Every row's arithmetic is the
+// leader's own, so results are unchanged.  While no warp of the block is
+// idle (all but the last queries) a leader only reads the idle count.
+struct PhaseDesc {
+  unsigned long long ticket;  // (generation << 32) | next group to take
+  unsigned long long gen_n;   // (generation << 32) | rows of the phase, one word
+  int q;                      // the phase's query
+  float qn;                   // its BF16 squared norm (tensor-core distances)
+  int done;                   // groups finished by helpers
+  int pad;
+};
+struct BlockShare {
+  unsigned int idle;          // warps of the block with no query left
+  unsigned int pad[3];
+  PhaseDesc desc[8];
+};
+static_assert(sizeof(BlockShare) == kBlockShareBytes, "block share layout");
+
+// The kernels that help in the tail: the tensor-core BF16 rows and the rows
+// of any chunk count, with batches of up to 64 slots.  The scalar register
+// path (FP32 and FP8 rows of up to 4 chunks, and 30 chunks) holds a group of
+// rows in registers, and a second copy of it for the helped phase made those
+// kernels spill at 64 registers.  Batches of 128 and 256 slots measured
+// slower helped (one ticket per group of 8 rows over 16-32 groups).
+template <int C, int PREC, int NB>
+__host__ __device__ constexpr bool tail_helping() {
+  return (C == 0 || (PREC == kPrecBF16 && C >= 1 && C <= 4)) && NB <= 2;
+}
+
+constexpr long long kHelpWaitLimit = 1ll << 24;   // leader's polls for helpers' groups
+constexpr long long kHelperIdleLimit = 1ll << 21; // empty scans (~0.4 s) before a helper leaves
+
+// The block's share, after its warps' regions (per_warp words each; a
+// multiple of 4, so 16-byte aligned).
+__device__ __forceinline__ BlockShare* block_share(uint32_t* smem, int per_warp) {
+  return reinterpret_cast<BlockShare*>(smem + (size_t)(blockDim.x >> 5) * per_warp);
+}
+
+// The leader's side of a helped distance phase.  Publishes (q, qn, n) and
+// the generation, takes groups from the ticket, then waits for the groups
+// helpers took (bounded; on timeout the error word is set).
+template <int C, int PREC>
+__device__ __forceinline__ void helped_distances(const SearchArgs& a, const float (&qv)[qregs(C)],
+                                                 const QueryExtra<C, PREC>& qx, const int* s_ids,
+                                                 float* s_dist, int n, int lane, int q, float qn,
+                                                 BlockShare* bs) {
+  constexpr int G = distance_group_size<C, PREC>();
+  PhaseDesc& d = bs->desc[threadIdx.x >> 5];
+  const int ng = (n + G - 1) / G;
+  if (lane == 0) {
+    const unsigned gen = (unsigned)(*reinterpret_cast<volatile unsigned long long*>(&d.gen_n) >> 32) + 1u;
+    d.q = q;
+    d.qn = qn;
+    d.done = 0;
+    *reinterpret_cast<volatile unsigned long long*>(&d.gen_n) = ((unsigned long long)gen << 32) | (unsigned)n;
+    __threadfence_block();
+    atomicExch(&d.ticket, (unsigned long long)gen << 32);
+  }
+  __syncwarp();
+  prefetch_batch<C, PREC>(a, s_ids, n, lane);
+  int mine = 0;
+  for (;;) {
+    unsigned long long old = 0;
+    if (lane == 0) old = atomicAdd(&d.ticket, 1ull);
+    const int grp = (int)__shfl_sync(kFull, (unsigned)old, 0);
+    if (grp >= ng) break;
+    distance_group<C, PREC>(a, qv, qx, s_ids, s_dist, n, lane, grp);
+    ++mine;
+  }
+  if (lane == 0) {
+    const int expect = ng - mine;  // every group below ng was taken by someone
+    long long it = 0;
+    while (*reinterpret_cast<volatile int*>(&d.done) < expect) {
+      if (++it > kHelpWaitLimit) {
+        if (a.err) atomicExch(a.err, kErrHelpWait);
+        break;
+      }
+    }
+    __threadfence_block();
+  }
+  __syncwarp();
+}
+
 template <int C, int PREC, bool TEAM = false>
 __device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)[qregs(C)],
                                           const QueryExtra<C, PREC>& qx, const int* s_ids,
@@ -737,17 +898,7 @@ __device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)
     const int first_rows = prefetch_first(n, kRowBytes, kAhead);
     prefetch_local<G>(rows, kRowBytes, kLines, s_ids, n, lane, ws, ks, 0, first_rows);
     const int first = G * ws, step = G * ks;
-    auto group = [&](int g0) {
-      // all G loads first, unconditionally (a short group re-reads its first
-      // row), so they are issued back to back before any use
-      RowLoader<C, PREC> r[G];
-#pragma unroll
-      for (int t = 0; t < G; ++t) r[t].load(a, s_ids[g0 + t < n ? g0 + t : g0], lane);
-      float part[G];
-#pragma unroll
-      for (int t = 0; t < G; ++t) part[t] = g0 + t < n ? lane_partial<C>(r[t].v, qv) : 0.0f;
-      reduce_rows<G>(part, s_dist, g0, n, lane);
-    };
+    auto group = [&](int g0) { regs_group<C, PREC>(a, qv, s_ids, s_dist, n, lane, g0); };
     // the window's loop is a copy of its own: the whole-batch loop keeps no
     // window state in the registers these rows fill
     if (first_rows >= n) {
@@ -765,12 +916,14 @@ __device__ __forceinline__ void distances(const SearchArgs& a, const float (&qv)
 // Compact the valid batch ids (0 <= id < np) into s_ids in slot order,
 // compute their distances, and scatter them back (invalid slots -> MAX).
 // With TEAM, the team's warps share the distances (team leader only).
+// Alone (not TEAM), with bs, idle warps of the block may help (tail).
 template <int C, int NB, int PREC, bool TEAM = false>
 __device__ __forceinline__ int batch_distances(const SearchArgs& a, const float (&qv)[qregs(C)],
                                                const QueryExtra<C, PREC>& qx,
                                                float (&bd)[batch_regs(NB)],
                                                const int (&bi)[batch_regs(NB)], int* s_ids,
-                                               float* s_dist, int lane, const Team& t = Team()) {
+                                               float* s_dist, int lane, const Team& t = Team(),
+                                               int q = 0, BlockShare* bs = nullptr) {
   constexpr int BR = batch_regs(NB);
   const unsigned lt = (1u << lane) - 1u;
   int kidx[BR];
@@ -790,7 +943,14 @@ __device__ __forceinline__ int batch_distances(const SearchArgs& a, const float 
     team_sync(t);
   } else {
     __syncwarp();
-    distances<C, PREC>(a, qv, qx, s_ids, s_dist, n, lane);
+    constexpr int G = distance_group_size<C, PREC>();
+    if (tail_helping<C, PREC, NB>() && bs && n > G && *reinterpret_cast<volatile unsigned*>(&bs->idle) != 0u) {
+      float qn = 0.0f;
+      if constexpr (PREC == kPrecBF16 && C >= 1 && C <= 4) qn = qx.qn;
+      if constexpr (tail_helping<C, PREC, NB>()) helped_distances<C, PREC>(a, qv, qx, s_ids, s_dist, n, lane, q, qn, bs);
+    } else {
+      distances<C, PREC>(a, qv, qx, s_ids, s_dist, n, lane);
+    }
     __syncwarp();
   }
 #pragma unroll
@@ -874,7 +1034,7 @@ __device__ __forceinline__ void load_query(const SearchArgs& a, int q, int lane,
 template <int C, int NL, int NB, int PREC, bool R16, bool TEAM = false>
 __device__ __forceinline__ void search_query(const SearchArgs& a, int q, int lane, const Bloom& bloom,
                                              int* s_ids, float* s_dist, uint32_t* q_slot,
-                                             const Team& t = Team()) {
+                                             const Team& t = Team(), BlockShare* bs = nullptr) {
   constexpr int L = pool_slots(NL);
   constexpr int PR = pool_regs(NL);  // pool registers
   constexpr int BR = batch_regs(NB);  // batch registers
@@ -954,7 +1114,7 @@ __device__ __forceinline__ void search_query(const SearchArgs& a, int q, int lan
       bi[j] = id;
     }
     __syncwarp();
-    c_entries += batch_distances<C, NB, PREC, TEAM>(a, qv, qx, bd, bi, s_ids, s_dist, lane, t);
+    c_entries += batch_distances<C, NB, PREC, TEAM>(a, qv, qx, bd, bi, s_ids, s_dist, lane, t, q, bs);
     if (batch_can_enter<NL, NB>(pd, bd)) {
       sort_batch_desc<BR, true, B, kMergeFrom>(bd, bi, lane);
       merge_pool<NL, NB>(pd, pi, bd, bi, false, lane);
@@ -1100,7 +1260,7 @@ __device__ __forceinline__ void search_query(const SearchArgs& a, int q, int lan
       }
     }
 
-    c_dists += batch_distances<C, NB, PREC, TEAM>(a, qv, qx, bd, bi, s_ids, s_dist, lane, t);
+    c_dists += batch_distances<C, NB, PREC, TEAM>(a, qv, qx, bd, bi, s_ids, s_dist, lane, t, q, bs);
     {
       // batch slots below the pool's largest distance: none -> the merge
       // changes nothing (batch_can_enter); a few distinct ones -> placed
@@ -1195,6 +1355,79 @@ __device__ __forceinline__ void help_query(const SearchArgs& a, int q, int lane,
   }
 }
 
+// A warp with no query left: helps the block's searching warps with their
+// distance phases until every warp of the block is idle (or, as a safety
+// bound, after kHelperIdleLimit scans that found nothing).  A group is taken
+// only through the leader's ticket, and only when the ticket's generation
+// matches the published (generation, rows) word read after taking it, so a
+// stale take of an ended phase is dropped; the leader cannot end a phase
+// while a group it counts on is being computed.
+template <int C, int NL, int NB, int PREC>
+__device__ __noinline__ void help_block(const SearchArgs a, uint32_t* smem, int per_warp, int lane,
+                                        BlockShare* bs) {
+  constexpr int G = distance_group_size<C, PREC>();
+  constexpr int S = batch_slots(NB) > pool_slots(NL) ? batch_slots(NB) : pool_slots(NL);
+  const int wpb = blockDim.x >> 5, me = threadIdx.x >> 5;
+  if (lane == 0) atomicAdd(&bs->idle, 1u);
+  __syncwarp();
+  float qv[qregs(C)];
+#pragma unroll
+  for (int c = 0; c < qregs(C); ++c) qv[c] = 0.0f;
+  QueryExtra<C, PREC> qx{};
+  long long empty = 0;
+  for (;;) {
+    if (*reinterpret_cast<volatile unsigned*>(&bs->idle) >= (unsigned)wpb) break;
+    bool worked = false;
+    for (int w = 0; w < wpb; ++w) {
+      if (w == me) continue;
+      PhaseDesc& d = bs->desc[w];
+      const unsigned long long t0 = *reinterpret_cast<volatile unsigned long long*>(&d.ticket);
+      const unsigned long long gn0 = *reinterpret_cast<volatile unsigned long long*>(&d.gen_n);
+      if ((t0 >> 32) == 0 || (t0 >> 32) != (gn0 >> 32)) continue;
+      if ((int)(unsigned)t0 >= ((int)(unsigned)gn0 + G - 1) / G) continue;
+      unsigned long long old = 0;
+      if (lane == 0) old = atomicAdd(&d.ticket, 1ull);
+      old = __shfl_sync(kFull, old, 0);
+      __threadfence_block();
+      const unsigned long long gn = *reinterpret_cast<volatile unsigned long long*>(&d.gen_n);
+      const unsigned gs = (unsigned)(old >> 32);
+      const int grp = (int)(unsigned)old;
+      const int n = (int)(unsigned)gn;
+      if (gs == 0u || gs != (unsigned)(gn >> 32) || grp >= (n + G - 1) / G) continue;
+      const int q = *reinterpret_cast<volatile int*>(&d.q);
+      uint32_t* lb = smem + (size_t)w * per_warp;  // the leader's region
+      const int* ls_ids = reinterpret_cast<const int*>(lb + a.bloom_words);
+      float* ls_dist = reinterpret_cast<float*>(lb + a.bloom_words + S);
+      const uint32_t* lslot = lb + a.bloom_words + 2 * S;
+      // the leader's query: its shared-memory row, or the FP32 chunks again
+      if constexpr (C == 0) {
+        qx.qs = reinterpret_cast<const float*>(lslot);
+      } else {
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          const int dim = lane + 32 * c;
+          qv[c] = dim < a.d ? __ldg(a.queries + (size_t)q * a.qstride + dim) : 0.0f;
+        }
+        if constexpr (PREC == kPrecBF16 && C <= 4) {
+          qx.qs = lslot;
+          qx.qn = *reinterpret_cast<volatile float*>(&d.qn);
+        }
+      }
+      distance_group<C, PREC>(a, qv, qx, ls_ids, ls_dist, n, lane, grp);
+      __syncwarp();
+      if (lane == 0) {
+        __threadfence_block();
+        atomicAdd(&d.done, 1);
+      }
+      worked = true;
+    }
+    if (!worked) {
+      __nanosleep(256);
+      if (++empty > kHelperIdleLimit) break;
+    }
+  }
+}
+
 // Blocks of 8 warps per SM the register budget is set for: 4 (64 registers
 // a thread), or 2 (128) for rows of more than 4 chunks in registers and for
 // the kernels built for any chunk count with a pool or batch of 8
@@ -1225,14 +1458,22 @@ __global__ void __launch_bounds__(256, search_min_blocks(C, NL, NB)) search_kern
   int* s_ids = reinterpret_cast<int*>(wbase + a.bloom_words);
   float* s_dist = reinterpret_cast<float*>(s_ids + S);
   const int nq = a.nq_dev ? *a.nq_dev : a.nq;
+  constexpr bool kHelps = tail_helping<C, PREC, NB>();
+  BlockShare* bs = nullptr;
+  if constexpr (kHelps) {
+    bs = block_share(smem, per_warp);
+    for (int i = threadIdx.x; i < kBlockShareBytes / 4; i += blockDim.x) reinterpret_cast<uint32_t*>(bs)[i] = 0u;
+    __syncthreads();
+  }
   for (;;) {
     int q = 0;
     if (lane == 0) q = (int)atomicAdd(a.work, 1u);
     q = __shfl_sync(kFull, q, 0);
     if (q >= nq) break;
     search_query<C, NL, NB, PREC, R16>(a, q, lane, bloom, s_ids, s_dist,
-                                       reinterpret_cast<uint32_t*>(s_dist + S));
+                                       reinterpret_cast<uint32_t*>(s_dist + S), Team(), bs);
   }
+  if constexpr (kHelps) help_block<C, NL, NB, PREC>(a, smem, per_warp, lane, bs);
 }
 
 // search_kernel with teams of K warps per query (Team): K = a.team, or,

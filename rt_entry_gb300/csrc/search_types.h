@@ -29,6 +29,12 @@ RTE_HD constexpr int query_slot_words_for(int C, int chunks) {
 // (a power of two >= 32 words), the compaction words (2 x 16..256) and the
 // query slot (64 or 32 x chunks words) are all multiples of 4 words.
 constexpr int kTeamCtlWords = 4;
+// Shared memory a search block keeps after its warps' regions: the tail
+// helping state (a count of idle warps and one phase descriptor per warp,
+// search_kernel.cuh's BlockShare).  Every launch reserves it.
+constexpr int kBlockShareBytes = 16 + 8 * 32;
+// Codes the search kernels write to SearchArgs::err when a bounded wait runs out.
+constexpr int kErrHelpWait = 3;
 constexpr int kMaxHits = 8;  // leaves per query for kd-tree entries
 constexpr int kMaxChunks = 32;  // rows of up to 1024 dims
 
@@ -55,6 +61,7 @@ struct SearchArgs {
   int C;                    // chunks of 32 dims per row (set by launch_search)
   int team;                 // warps per query: 0 or 1 alone, 2/4/8 a team, < 0 chosen
                             // by the kernel from the live query count, at least -team
+  int* err;                 // device word set to a non-zero code when a bounded wait runs out, or null
 };
 
 }  // namespace rte

@@ -130,7 +130,7 @@ rte_status capture(rte_batcher* b) {
     cudaError_t ej = cudaStreamWaitEvent(st, b->join, 0);
     if (e == cudaSuccess) e = ej;
   } else {
-    e = cudaMemsetAsync(b->dwork.p, 0, sizeof(unsigned int), st);
+    e = cudaMemsetAsync(b->dwork.p, 0, 2 * sizeof(unsigned int), st);
     if (e == cudaSuccess && x->has_pca) {
       e = launch_project_dyn(b->dq.p, b->cap, b->dn.p, x->dim, x->dim, x->d_mean.p, x->d_rot.p,
                              x->search_dim, x->search_dim, b->dproj.p, x->search_dim, st,
@@ -174,6 +174,9 @@ rte_status capture(rte_batcher* b) {
     // automatic teams follow the live batch size, which the graph reads on
     // the device; the grid, planned for the capacity, leaves them room
     a.team = b->prm.team_warps == 0 ? -team_floor(b->prm.precision, L, wpb) : team;
+    // bounded waits report into the head's error word (learned entries) or
+    // the word after the work counter
+    a.err = learned ? reinterpret_cast<int*>(b->dzero.p + b->cap * 2) : reinterpret_cast<int*>(b->dwork.p + 1);
     e = launch_search(a, x->C, NL, NB, b->prm.precision, wpb, grid, smem, st);
   }
   cudaError_t e2 = cudaStreamEndCapture(st, &b->graph);
@@ -226,7 +229,7 @@ extern "C" rte_status rte_batcher_create(rte_index* x, int64_t max_nq,
       b->dproj.alloc((size_t)max_nq * x->search_dim) != cudaSuccess ||
       b->dhits.alloc(max_nq) != cudaSuccess || b->dids.alloc((size_t)max_nq * kmax) != cudaSuccess ||
       b->ddist.alloc((size_t)max_nq * kmax) != cudaSuccess || b->dn.alloc(1) != cudaSuccess ||
-      b->dwork.alloc(1) != cudaSuccess || cudaMallocHost(&b->hn, sizeof(int)) != cudaSuccess)
+      b->dwork.alloc(2) != cudaSuccess || cudaMallocHost(&b->hn, sizeof(int)) != cudaSuccess)
     return bail(fail(RTE_ENOMEM, "batcher buffers"));
   if (params->entry_mode == RTE_ENTRY_LEARNED &&
       (b->dhits2.alloc(max_nq) != cudaSuccess || b->dxb.alloc((size_t)max_nq * x->mlp.dp) != cudaSuccess ||

@@ -199,6 +199,29 @@ def test_teams_match_single_warp_and_oracle(lib, orc, cuda, d, integer, R, L, W,
         assert np.array_equal(ids1, oids) and np.array_equal(d1, od)
 
 
+# Helping in the tail: one warp per query (team_warps = 1); warps left
+# without a query share the distance phases of their block's searching
+# warps.  A batch of 37 queries leaves idle warps in a block from the start;
+# 700 gives a tail.  Integer data: bit-exact with the oracle.
+@pytest.mark.parametrize("d,prec,rerank,W", [(128, 1, 1, 1), (128, 1, 0, 2), (160, 0, 0, 1), (160, 1, 1, 1)])
+@pytest.mark.parametrize("nq", [37, 700])
+def test_tail_helping_matches_oracle(lib, orc, cuda, d, prec, rerank, W, nq):
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(3000, nq, d, True, seed=d + prec + rerank + nq)
+    graph = ds.knn_graph(base, 64)
+    idx = _index(base, graph, 32, 0.2)
+    _, _, pids = idx.kdtree()
+    hits = idx.locate(q)
+    kw = dict(beam=32, k=32, search_width=W, precision=prec, rerank=rerank, team_warps=1)
+    ids, dd = idx.search_projected(q, **kw)
+    low = idx.search_base_lowp(prec) if prec else base
+    oids, od, ocnt = orc.search(low, q, graph, L=32, k=32, search_width=W, leaf_pids=pids, hits=hits,
+                                rerank_base=base if rerank else None, with_counters=True)
+    assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
+    assert np.array_equal(dd, od)
+    assert np.array_equal(idx.counters(q, **kw), ocnt[:, :4])
+
+
 def test_automatic_teams_on_small_batches(lib, cuda):
     """team_warps = 0 spreads a small batch over up to 8 warps per query (and
     a large one over one): same results as one warp per query, for batches
