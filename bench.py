@@ -871,8 +871,8 @@ def main():
                "e2e": {"value": e2e, "unit": "queries/s",
                        "h2d_bytes_per_step": int(nq * d * 4),
                        "d2h_bytes_per_step": int(nq * K_TOP * 8)},
-               # per timed step of the headline arm: project_rows, locate_points (side
-               # stream), mlp_head_kernel, locate_in_subtree_wide, search_kernel
+               # per timed step of the headline arm: project_tf32_kernel, locate_points
+               # (side stream), mlp_head_kernel, locate_in_subtree_wide, search_kernel
                "gpu_launches": 5 * args.steps,
                "clocks": clocks}
         det = json.dumps(B.details)
