@@ -136,7 +136,12 @@ rte_status rte_locate(rte_index* idx, const float* projected, int64_t nq, int32_
 /* The whole query path (Graph::Search, graph.cu:254-293): projection, entry
  * selection, beam search (GraphSearchKernel, graph_search.cuh:56-1964).
  * out_ids [nq x k] (|pool id|, np for an empty slot), out_dists [nq x k]
- * squared L2 in the search space (536870912.0f for an empty slot) or NULL. */
+ * squared L2 in the search space (536870912.0f for an empty slot) or NULL.
+ * With host buffers the call returns when the results are in them, and
+ * RTE_ETIMEOUT if a bounded device wait in the path ran out (the learned
+ * head's pipeline, or a search warp waiting on the block's tail helpers);
+ * with device buffers the call is asynchronous and such a wait only sets
+ * a device word.  The same holds for rte_search_projected. */
 rte_status rte_search(rte_index* idx, const float* queries, int64_t nq,
                       const rte_search_params* params, int32_t* out_ids, float* out_dists,
                       void* stream);
