@@ -85,7 +85,9 @@ def test_noalloc_search_equals_allocating_search(lib, cuda):
     for kw, hits in ((dict(beam=64, k=10), None),
                      (dict(beam=128, k=128, precision=r.PREC_BF16, rerank=1), None),
                      (dict(beam=32, k=16, entry_mode=r.ENTRY_RANDOM), None),
-                     (dict(beam=32, k=10), leaves)):
+                     (dict(beam=32, k=10), leaves),
+                     # one warp per query: the single-warp kernel and its tail helping
+                     (dict(beam=32, k=10, precision=r.PREC_BF16, rerank=1, team_warps=1), None)):
         params = r.default_params(**kw)
         want_ids, want_d = idx.search_projected(qp, hits=hits, params=params)
         torch.cuda.synchronize()
