@@ -206,12 +206,14 @@ def _boundary_rows(D, kth, tol, kk):
 
 
 def knn_graph(base: np.ndarray, R: int, device: str | None = None, chunk: int = 4096) -> np.ndarray:
-    """Exact degree-R kNN graph (self excluded), rows ordered by (dist, id).
-    Candidates come from approximate distances |x|^2 + |y|^2 - 2 x.y (FP32 on
-    a device, FP64 on the host) with a bound tol on their error; rows whose
-    candidate cut falls inside a run of (near-)equal distances are redone
-    over the whole run, so many equal distances (duplicated rows) still give
-    the smallest ids."""
+    """Degree-R kNN graph (self excluded), rows ordered by (FP64 dist, id).
+    Candidates come from approximate distances |x|^2 + |y|^2 - 2 x.y, then
+    an FP64 rerank.  On the host (FP64) the result is exact: rows whose
+    candidate cut falls within the FP64 error bound of other columns are
+    redone over all of them.  On a device (FP32) the candidates are the
+    R + 8 smallest, and only runs of exactly equal FP32 distances at the cut
+    (duplicated rows) are widened; this library's rte_knn_graph is the
+    certified exact builder on the GPU."""
     n, d = base.shape
     if n <= R:
         raise ValueError("need more than R base vectors")
@@ -226,7 +228,6 @@ def knn_graph(base: np.ndarray, R: int, device: str | None = None, chunk: int = 
             X = torch.from_numpy(base).to(dev)
             nrm64 = (X.double() ** 2).sum(1)
             nrm_d = nrm64.float()
-            nmax = float(nrm64.max())
             for s in range(0, n, chunk):
                 e = min(n, s + chunk)
                 D = nrm_d[s:e, None] + nrm_d[None, :] - 2.0 * (X[s:e] @ X.T)
@@ -237,10 +238,11 @@ def knn_graph(base: np.ndarray, R: int, device: str | None = None, chunk: int = 
                 dd = ((cand - X[s:e, None, :].double()) ** 2).sum(-1)
                 dd_np, iv_np = _sort_by_dist_then_id(dd.cpu().numpy(), iv.cpu().numpy())
                 out[s:e] = iv_np[:, :R]
-                # FP32 products and sums: error below (d + 2) 2^-22 (|x|^2 + |y|^2);
-                # the cut at kth + 4 tol leaves room for its own FP32 rounding
-                tol = ((d + 2) * 2.0 ** -22 * (nrm64[s:e] + nmax)).float()
-                thr = dv[:, -1] + 4 * tol
+                # rows whose cut falls inside a run of equal FP32 distances
+                # (duplicated rows): redone over the whole run.  Near-ties
+                # are left to the R + 8 candidates, as a bound of the FP32
+                # error would pull in most rows of a dense base.
+                thr = dv[:, -1]
                 cnt = (D <= thr[:, None]).sum(1)
                 over = (cnt > kk).nonzero().flatten()
                 if over.numel():  # redo those rows over every column below the cut
