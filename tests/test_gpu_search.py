@@ -203,12 +203,13 @@ def test_teams_match_single_warp_and_oracle(lib, orc, cuda, d, integer, R, L, W,
 # without a query share the distance phases of their block's searching
 # warps.  A batch of 37 queries leaves idle warps in a block from the start;
 # 700 gives a tail.  Integer data: bit-exact with the oracle.
-@pytest.mark.parametrize("d,prec,rerank,W", [(128, 1, 1, 1), (128, 1, 0, 2), (160, 0, 0, 1), (160, 1, 1, 1)])
+@pytest.mark.parametrize("d,prec,rerank,W,R", [(128, 1, 1, 1, 64), (128, 1, 0, 2, 64), (160, 0, 0, 1, 64),
+                                              (160, 1, 1, 1, 64), (128, 1, 1, 1, 16), (160, 0, 0, 2, 16)])
 @pytest.mark.parametrize("nq", [37, 700])
-def test_tail_helping_matches_oracle(lib, orc, cuda, d, prec, rerank, W, nq):
+def test_tail_helping_matches_oracle(lib, orc, cuda, d, prec, rerank, W, R, nq):
     from rt_entry_gb300 import datasets as ds
-    base, q = _mixture(3000, nq, d, True, seed=d + prec + rerank + nq)
-    graph = ds.knn_graph(base, 64)
+    base, q = _mixture(3000, nq, d, True, seed=d + prec + rerank + nq + R)
+    graph = ds.knn_graph(base, R)
     idx = _index(base, graph, 32, 0.2)
     _, _, pids = idx.kdtree()
     hits = idx.locate(q)
