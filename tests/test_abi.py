@@ -32,6 +32,26 @@ def test_default_params(lib):
     assert p.entry_mode == r.ENTRY_KDTREE and p.precision == r.PREC_FP32
 
 
+def test_search_params_layout_matches_the_header(lib):
+    """The ctypes struct has the header's fields in the header's order, and
+    rte_default_params writes exactly that many bytes."""
+    import ctypes
+    import re
+
+    import rt_entry_gb300 as r
+    text = open(os.path.join(ROOT, "include", "rtentry.h")).read()
+    body = re.search(r"typedef struct \{(.*?)\} rte_search_params;", text, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = re.findall(r"\bint\s+(\w+)\s*;", body)
+    assert fields == [f for f, _ in r.SearchParams._fields_]
+    n = ctypes.sizeof(r.SearchParams)
+    buf = (ctypes.c_ubyte * (n + 64))(*([0xA5] * (n + 64)))
+    lib.rte_default_params(ctypes.cast(buf, ctypes.POINTER(r.SearchParams)))
+    assert bytes(buf[n:]) == bytes([0xA5] * 64), "rte_default_params wrote past the struct"
+    p = r.SearchParams.from_buffer_copy(bytes(buf[:n]))
+    assert p.team_warps == 0 and p.max_hits == 1
+
+
 def test_null_and_bad_arguments_return_status(lib):
     import rt_entry_gb300 as r
     h = ctypes.c_void_p()
