@@ -341,12 +341,12 @@ class Bench:
         return out
 
 
-def reference_kernel_bench(B, idx, qp, hits, graph, steps):
+def reference_kernel_bench(B, idx, qp, hits, graph, steps, beams=(32, 16)):
     """The reference's GraphSearchKernel (compiled from its own
     graph_search.cuh for sm_103a, launched <<<nq, 64>>> as graph.cu:320-324
     does) against this library's search kernel on identical projected
     queries, hits, graph and entry table: FP32, kd-tree entries, width 1,
-    k = 10, at beams 32 and 16.  ids_differ counts queries whose ten ids
+    k = 10, at the given beams (config 2: 32 and 16).  ids_differ counts queries whose ten ids
     differ over the full batch (the reference's never-cleared shared bloom
     filter lets a block inherit bits from the previous block on its SM);
     scrubbed_200_equal compares the first 200 queries run one launch each on
@@ -362,7 +362,7 @@ def reference_kernel_bench(B, idx, qp, hits, graph, steps):
     out = {"launch": "<<<nq, 64>>>, graph_search.cuh built with --use_fast_math -O3 for sm_103a"}
     rk = oracle.RefKernel(pb, graph)
     try:
-        for L in (32, 16):
+        for L in beams:
             ent = oracle.entries_table(pids, L, pb.shape[0])
             ref_ids, ref_ms = rk.search(qp_np, ent, hits_np, L, K_TOP, reps=steps)
             p = r.default_params(beam=L, k=K_TOP)
@@ -371,9 +371,17 @@ def reference_kernel_bench(B, idx, qp, hits, graph, steps):
             our_ms = statistics.median(B.time_kernel(idx, qp, hits, p, steps, B.args.warmup))
             sc_ids, _ = rk.search(qp_np[:200], ent, hits_np[:200], L, K_TOP, scrub=True)
             rms = statistics.median(ref_ms)
+            # both kernels evaluate the same rows (the same algorithm; only the
+            # queries counted in ids_differ can take other paths), so one
+            # count of algorithmic bytes serves both fractions of the HBM peak
+            cnt = idx.counters(qp, hits=hits, params=p)
+            alg = algorithmic_bytes(cnt, d, L, graph.shape[1], K_TOP)
             out[f"beam{L}"] = {"ref_ms": round(rms, 4), "ref_qps": round(nq / (rms / 1000.0)),
                                "ours_ms": round(our_ms, 4), "ours_qps": round(nq / (our_ms / 1000.0)),
                                "speedup": round(rms / our_ms, 2),
+                               "alg_bytes": alg,
+                               "ref_frac": round(alg / (rms / 1000.0) / 1e9 / B.hbm, 3),
+                               "ours_frac": round(alg / (our_ms / 1000.0) / 1e9 / B.hbm, 3),
                                "ids_differ": int((ref_ids != ours).any(1).sum()),
                                "scrubbed_200_equal": bool(np.array_equal(sc_ids, ours[:200]))}
             B.log(f"reference kernel beam {L}: {out[f'beam{L}']}")
@@ -566,6 +574,8 @@ def other_config(B, cfg, n4):
                                                  rerank=1)
     cpu, _ = cpu_sample_qps(idx, w.graph, qp.cpu().numpy(), hits.cpu().numpy(), plain["beam"],
                             plain["width"], n=1000 if cfg != 3 else 300)
+    # the reference's own kernel at 960 dimensions beside this library's
+    ref_kernel = reference_kernel_bench(B, idx, qp, hits, w.graph, 3, beams=(256, 64)) if cfg == 3 else None
     prec = precision_table(B, idx, w, nq=1000 if cfg == 3 else 2000)
     names = {1: "100k x 128 isotropic 64-cluster mixture (sigma 5), 10k queries, exact degree-32 graph, "
                 "PCA-128 (kd-tree on the first 3), leaf 32",
@@ -576,6 +586,8 @@ def other_config(B, cfg, n4):
                 f"learned head trained on 1M queries"}
     out = {"workload": names[cfg], "arms": arms, "cpu_baseline": cpu, "precision": prec,
            "setup_s": round(setup, 1), "index_build_s": round(build, 1)}
+    if ref_kernel is not None:
+        out["reference_kernel_gb300"] = ref_kernel
     if train_s is not None:
         out["train_s"] = train_s
     if cfg == 1:
