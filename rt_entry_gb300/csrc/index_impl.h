@@ -19,6 +19,14 @@ rte_status fail(rte_status s, const std::string& msg);
 rte_status ensure_precision(rte_index* x, int precision);
 void clear_error();
 bool is_device_ptr(const void* p);
+// Launch plan of a search of nq queries (api.cpp): pool and batch shape,
+// warps per block, grid, shared memory and warps per query; *ordered is
+// set when the batch outnumbers the resident warps and has entry leaves, so
+// that taking its queries in leaf order (launch_order_by_leaf) pays.
+rte_status search_plan(const rte_index* x, const rte_search_params* prm, int64_t nq, int* L, int* k,
+                       int* NL, int* NB, int* wpb, int* grid, size_t* smem, int* team, bool* ordered);
+// The fewest warps per query that automatic teams use (api.cpp).
+int team_floor(int prec, int L, int wpb);
 
 #define RTE_CUDA(call)                                                                     \
   do {                                                                                     \

@@ -747,4 +747,95 @@ cudaError_t launch_locate_dyn(const WideNode* wide, int n_wide, const float* pts
   return cudaGetLastError();
 }
 
+// Counting sort of the queries by leaf range: count per range, exclusive
+// scan of the counts, then scatter.  Shared-memory atomics: 4096 counters
+// leave few collisions for batches of up to a few hundred thousand queries.
+constexpr int kOrderBins = 4096;
+constexpr int kOrderThreads = 1024;
+constexpr int kOrderKeys = 16;
+
+__device__ __forceinline__ int order_bin(int32_t leaf, int n_leaves) {
+  if (leaf < 0 || leaf >= n_leaves) leaf = 0;
+  return (int)(((int64_t)leaf * kOrderBins) / n_leaves);
+}
+
+__global__ void __launch_bounds__(kOrderThreads) order_by_leaf_kernel(const int32_t* __restrict__ leaf,
+                                                                      int stride, int64_t n, int n_leaves,
+                                                                      int32_t* __restrict__ order) {
+  __shared__ int cnt[kOrderBins];
+  __shared__ int wsum[kOrderThreads / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < kOrderBins; i += kOrderThreads) cnt[i] = 0;
+  __syncthreads();
+  // each thread issues kOrderKeys independent loads per round, so that a
+  // batch of up to kOrderKeys * 1024 queries costs one memory latency per
+  // pass rather than a chain of them
+  for (int64_t r0 = 0; r0 < n; r0 += (int64_t)kOrderKeys * kOrderThreads) {
+    int b[kOrderKeys];
+#pragma unroll
+    for (int j = 0; j < kOrderKeys; ++j) {
+      const int64_t q = r0 + (int64_t)j * kOrderThreads + tid;
+      b[j] = q < n ? order_bin(leaf[q * stride], n_leaves) : -1;
+    }
+#pragma unroll
+    for (int j = 0; j < kOrderKeys; ++j)
+      if (b[j] >= 0) atomicAdd(&cnt[b[j]], 1);
+  }
+  __syncthreads();
+  // exclusive scan: thread t owns the ranges [per * t, per * t + per)
+  constexpr int per = kOrderBins / kOrderThreads;
+  int v[per];
+  int own = 0;
+#pragma unroll
+  for (int j = 0; j < per; ++j) {
+    v[j] = cnt[tid * per + j];
+    own += v[j];
+  }
+  int inc = own;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    const int w = wsum[lane];
+    int wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    wsum[lane] = wi - w;
+  }
+  __syncthreads();
+  int at = wsum[warp] + inc - own;
+#pragma unroll
+  for (int j = 0; j < per; ++j) {
+    cnt[tid * per + j] = at;
+    at += v[j];
+  }
+  __syncthreads();
+  for (int64_t r0 = 0; r0 < n; r0 += (int64_t)kOrderKeys * kOrderThreads) {
+    int b[kOrderKeys];
+#pragma unroll
+    for (int j = 0; j < kOrderKeys; ++j) {
+      const int64_t q = r0 + (int64_t)j * kOrderThreads + tid;
+      b[j] = q < n ? order_bin(leaf[q * stride], n_leaves) : -1;
+    }
+#pragma unroll
+    for (int j = 0; j < kOrderKeys; ++j)
+      if (b[j] >= 0) order[atomicAdd(&cnt[b[j]], 1)] = (int32_t)(r0 + (int64_t)j * kOrderThreads + tid);
+  }
+}
+
+cudaError_t launch_order_by_leaf(const int32_t* leaf, int stride, int64_t n, int n_leaves,
+                                 int32_t* order, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  if (n > INT32_MAX || n_leaves < 1 || stride < 1) return cudaErrorInvalidValue;
+  order_by_leaf_kernel<<<1, kOrderThreads, 0, st>>>(leaf, stride, n, n_leaves, order);
+  return cudaGetLastError();
+}
+
 }  // namespace rte

@@ -120,5 +120,15 @@ cudaError_t launch_locate_multi(const WideNode* wide, int n_wide, const float* p
 // memory.
 cudaError_t launch_locate(const WideNode* wide, int n_wide, const float* pts, int64_t n, int stride,
                           int32_t* out, cudaStream_t st, bool top_cache = true);
+// The order in which a search takes its queries: a permutation of [0, n)
+// grouping queries by entry leaf (leaf[i * stride]; a leaf outside
+// [0, n_leaves) counts as leaf 0, the search's own fallback).  Leaves are
+// numbered in the kd-tree build's depth-first order, so queries close in
+// the order start in nearby parts of the base, and the queries a persistent
+// search runs at the same time then share more graph rows and vectors in
+// L2.  Within one of the 4096 leaf ranges the order is that of the atomic
+// counters; each query's result does not depend on it.  One block.
+cudaError_t launch_order_by_leaf(const int32_t* leaf, int stride, int64_t n, int n_leaves,
+                                 int32_t* order, cudaStream_t st);
 
 }  // namespace rte

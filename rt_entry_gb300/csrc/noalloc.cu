@@ -8,9 +8,9 @@
 // forbids third-party libraries to allocate behind its back.  For them
 // rte_search_projected_noalloc runs the entry-point location and the beam
 // search with every buffer supplied: the caller passes the inputs and the
-// outputs, and the only scratch the two kernels need -- the leaf of each
-// query and the work-queue counter of the persistent search -- lives in the
-// file-scope array below.  The array is reserved on a device when an index
+// outputs, and the only scratch the kernels need -- the leaf of each query,
+// the order in which the persistent search takes them and its work-queue
+// counter -- lives in the file-scope array below.  The array is reserved on a device when an index
 // is first created there (noalloc_prepare; with lazy module loading the
 // address lookup is what loads it) and kept until the process exits.
 #include <cuda_runtime.h>
@@ -21,11 +21,6 @@
 #include "index_kernels.h"
 #include "search_dispatch.h"
 
-namespace rte {
-rte_status search_plan(const rte_index* x, const rte_search_params* prm, int64_t nq, int* L, int* k,
-                       int* NL, int* NB, int* wpb, int* grid, size_t* smem, int* team);
-}  // namespace rte
-
 using namespace rte;
 
 namespace {
@@ -34,10 +29,12 @@ namespace {
 constexpr int kMaxQueries = 65536;
 
 // [0, 256): the search's work counter (first 4 bytes) and its error word
-// (next 4: a bounded wait ran out); [256, ...): hits.
+// (next 4: a bounded wait ran out); then the leaf and the place in the
+// search order of each query.
 struct NoallocScratch {
   unsigned int counter[64];
   int32_t hits[kMaxQueries];
+  int32_t order[kMaxQueries];
 };
 
 // Every GPU that loads the library holds this array until the process exits.
@@ -95,7 +92,8 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   // rte_search_projected does
   int L, k, NL, NB, wpb, grid, team;
   size_t smem;
-  rte_status s = search_plan(x, params, nq, &L, &k, &NL, &NB, &wpb, &grid, &smem, &team);
+  bool ordered = false;
+  rte_status s = search_plan(x, params, nq, &L, &k, &NL, &NB, &wpb, &grid, &smem, &team, &ordered);
   if (s != RTE_OK) return s;
   if (params->rerank == 2)
     return fail(RTE_EINVAL, "rerank 2 needs the original queries: use rte_search");
@@ -118,6 +116,11 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   if (params->entry_mode == RTE_ENTRY_KDTREE && !h) {
     RTE_CUDA(launch_locate(x->d_wide.p, (int)x->d_wide.n, projected, nq, x->search_dim, scr->hits, st));
     h = scr->hits;
+  }
+  const int32_t* order = nullptr;
+  if (ordered && params->entry_mode == RTE_ENTRY_KDTREE) {
+    RTE_CUDA(launch_order_by_leaf(h, 1, nq, (int)x->kd.n_leaves, scr->order, st));
+    order = scr->order;
   }
   // the array keeps the previous call's contents: the counter and the error
   // word must restart at 0
@@ -154,6 +157,7 @@ extern "C" rte_status rte_search_projected_noalloc(rte_index* x, const float* pr
   a.n_leaves = x->has_kdtree ? (int)x->kd.n_leaves : 1;
   a.max_hits = 1;
   a.team = team;
+  a.order = order;
   RTE_CUDA(launch_search(a, x->C, NL, NB, params->precision, wpb, grid, smem, st));
   return RTE_OK;
 }

@@ -1438,6 +1438,14 @@ __host__ __device__ constexpr int search_min_blocks(int C, int NL, int NB) {
   return C > 4 || (C == 0 && (NL >= 8 || NB >= 8)) ? 2 : 4;
 }
 
+// The next query of the persistent loop (one lane): the work counter's
+// next slot, through the order permutation when there is one; nq or more
+// once every query is taken.
+__device__ __forceinline__ int next_query(const SearchArgs& a, int nq) {
+  const int t = (int)atomicAdd(a.work, 1u);
+  return a.order && t < nq ? __ldg(a.order + t) : t;
+}
+
 template <int C, int NL, int NB, int PREC, bool R16 = false>
 __global__ void __launch_bounds__(256, search_min_blocks(C, NL, NB)) search_kernel(SearchArgs a) {
   extern __shared__ uint32_t smem[];
@@ -1467,7 +1475,7 @@ __global__ void __launch_bounds__(256, search_min_blocks(C, NL, NB)) search_kern
   }
   for (;;) {
     int q = 0;
-    if (lane == 0) q = (int)atomicAdd(a.work, 1u);
+    if (lane == 0) q = next_query(a, nq);
     q = __shfl_sync(kFull, q, 0);
     if (q >= nq) break;
     search_query<C, NL, NB, PREC, R16>(a, q, lane, bloom, s_ids, s_dist,
@@ -1523,7 +1531,7 @@ __global__ void __launch_bounds__(256, search_min_blocks(C, NL, NB)) search_kern
   if (t.w == 0) {
     for (;;) {
       int q = 0;
-      if (lane == 0) q = (int)atomicAdd(a.work, 1u);
+      if (lane == 0) q = next_query(a, nq);
       q = __shfl_sync(kFull, q, 0);
       if (lane == 0) t.ctl[0] = q;
       team_sync(t);

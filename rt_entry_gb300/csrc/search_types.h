@@ -62,6 +62,7 @@ struct SearchArgs {
   int team;                 // warps per query: 0 or 1 alone, 2/4/8 a team, < 0 chosen
                             // by the kernel from the live query count, at least -team
   int* err;                 // device word set to a non-zero code when a bounded wait runs out, or null
+  const int32_t* order;     // [nq] the order in which queries are taken (a permutation), or null
 };
 
 }  // namespace rte

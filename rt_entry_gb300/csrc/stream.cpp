@@ -29,12 +29,6 @@
 #include "rtentry.h"
 #include "search_dispatch.h"
 
-namespace rte {
-rte_status search_plan(const rte_index* x, const rte_search_params* prm, int64_t nq, int* L, int* k,
-                       int* NL, int* NB, int* wpb, int* grid, size_t* smem, int* team);
-int team_floor(int prec, int L, int wpb);
-}
-
 using namespace rte;
 
 struct rte_batcher {
@@ -71,7 +65,7 @@ rte_status capture(rte_batcher* b) {
   rte_index* x = b->idx;
   int L, k, NL, NB, wpb, grid, team;
   size_t smem;
-  rte_status s = search_plan(x, &b->prm, b->cap, &L, &k, &NL, &NB, &wpb, &grid, &smem, &team);
+  rte_status s = search_plan(x, &b->prm, b->cap, &L, &k, &NL, &NB, &wpb, &grid, &smem, &team, nullptr);
   if (s != RTE_OK) return s;
   b->k = k;
   RTE_CUDA(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));

@@ -158,6 +158,16 @@ def test_learned_entry_trains_and_searches(lib, orc, cuda):
                           hits2=kd)
     assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
     assert np.array_equal(dd, od)
+    # 12,000 queries at two warps each outnumber the resident warps: the
+    # batch is taken in kd-tree-leaf order, ordered on the side stream beside
+    # the model, and the results are still the oracle's
+    qb = mix.sample(12000, ds.SEED_QUERY + 5)
+    ib, db = idx.search(qb, beam=16, k=16, entry_mode=r.ENTRY_LEARNED)
+    qbp = idx.project(qb)
+    oids, od = orc.search(pb, qbp, graph, L=16, k=16, entry_mode=2, leaf_pids=pids,
+                          hits=idx.learned_leaves(qbp), hits2=idx.locate(qbp))
+    assert np.array_equal(ib, oids), f"{(ib != oids).any(1).sum()} queries differ"
+    assert np.array_equal(db, od)
     # the model's leaf alone, without the kd-tree leaf, is a usable entry
     # (a model mapped to the wrong leaves scores near zero here)
     rk, _ = idx.search(q, beam=32, k=10)

@@ -223,6 +223,32 @@ def test_tail_helping_matches_oracle(lib, orc, cuda, d, prec, rerank, W, R, nq):
     assert np.array_equal(idx.counters(q, **kw), ocnt[:, :4])
 
 
+# Batches larger than the resident warps (at most 4,864 on 152 SMs at these
+# shapes) are taken in entry-leaf order: the results stay those of the
+# oracle, which takes the queries one by one in index order.  Both single
+# leaves and the first of several leaves per query order the batch.
+@pytest.mark.parametrize("prec,rerank,H", [(0, 0, 1), (1, 1, 1), (0, 0, 2)])
+def test_leaf_ordered_large_batches_match_oracle(lib, orc, cuda, prec, rerank, H):
+    from rt_entry_gb300 import datasets as ds
+    base, q = _mixture(4000, 20000, 128, True, seed=90 + prec + H)
+    graph = ds.knn_graph(base, 64)
+    idx = _index(base, graph, 32, 0.2)
+    _, _, pids = idx.kdtree()
+    kw = dict(beam=32, k=10, precision=prec, rerank=rerank, max_hits=H)
+    ids, dd = idx.search_projected(q, **kw)
+    low = idx.search_base_lowp(prec) if prec else base
+    hits = idx.locate(q, max_hits=H)
+    if H > 1:
+        oids, od, ocnt = orc.search_multi(low, q, graph, L=32, k=10, hits_multi=hits, leaf_pids=pids,
+                                          with_counters=True)
+    else:
+        oids, od, ocnt = orc.search(low, q, graph, L=32, k=10, leaf_pids=pids, hits=hits,
+                                    rerank_base=base if rerank else None, with_counters=True)
+    assert np.array_equal(ids, oids), f"{(ids != oids).any(1).sum()} queries differ"
+    assert np.array_equal(dd, od)
+    assert np.array_equal(idx.counters(q, **kw), ocnt[:, :4])
+
+
 def test_automatic_teams_on_small_batches(lib, cuda):
     """team_warps = 0 spreads a small batch over up to 8 warps per query (and
     a large one over one): same results as one warp per query, for batches

@@ -109,6 +109,35 @@ def test_noalloc_search_equals_allocating_search(lib, cuda):
                 assert torch.cuda.mem_get_info()[0] == free0, "the call changed the free device memory"
 
 
+def test_noalloc_large_batch_in_leaf_order(lib, cuda):
+    """20,000 queries outnumber the resident warps, so both entry points take
+    them in entry-leaf order (the order lives in the fixed scratch here):
+    the same ids and distances as the allocating search, whose large batches
+    are checked against the oracle, with the library's own leaves and with
+    leaves the caller supplies."""
+    import torch
+
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+
+    base, q = _data(n=6000, nq=20000, seed=23)
+    graph = ds.knn_graph(base, 64)
+    idx = r.Index.from_arrays(base, graph).build_pca().build_kdtree(32, 0.2)
+    qp = idx.project(torch.from_numpy(q).cuda())
+    nq = qp.shape[0]
+    leaves = idx.locate(qp)
+    for kw, hits in ((dict(beam=32, k=10), None),
+                     (dict(beam=16, k=10, precision=r.PREC_BF16, rerank=1), leaves)):
+        params = r.default_params(**kw)
+        want_ids, want_d = idx.search_projected(qp, hits=hits, params=params)
+        ids = torch.full((nq, 10), -7, dtype=torch.int32, device="cuda")
+        dd = torch.full((nq, 10), float("nan"), dtype=torch.float32, device="cuda")
+        rc, ids, dd = _noalloc(lib, idx, qp, hits, params, nq, ids, dd)
+        assert rc == r.RTE_OK, lib.rte_last_error()
+        assert torch.equal(ids, want_ids), kw
+        assert torch.equal(dd, want_d), kw
+
+
 def test_noalloc_rejects_what_it_cannot_serve(lib, cuda):
     import torch
 
