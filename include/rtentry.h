@@ -164,8 +164,9 @@ rte_status rte_search_projected(rte_index* idx, const float* projected, const in
  *   - a BF16 or FP8 search needs that copy to exist already
  *     (rte_index_prepare, or an earlier search): RTE_ESTATE otherwise;
  *   - at most RTE_NOALLOC_MAX_QUERIES queries per call (RTE_EINVAL beyond);
- *   - its scratch (each query's leaf and the search's work counter, about
- *     256 KB) is one fixed array inside the library that every GPU holds
+ *   - its scratch (each query's leaf, the order in which a large batch's
+ *     queries are taken, and the search's work counter: about 512 KB) is
+ *     one fixed array inside the library that every GPU holds
  *     until the process exits.  Creating an index on a device
  *     (rte_index_from_host, rte_index_load, rte_index_load_dir) looks up the
  *     array's device address there, which is when the GPU reserves it (CUDA
@@ -211,8 +212,9 @@ typedef struct {
  * candidate runs on the sample queries [nq x dim]; recall@k is measured
  * against gt [nq x gt_k] (true neighbour ids, gt_k >= k); the fastest
  * candidate reaching target_recall wins (else the one with the best
- * recall).  Other fields of *params (precision, entry mode, max_iter,
- * hashes) are kept. */
+ * recall), where 4 warps per block must beat 8 by more than 3 % (8 leave
+ * room for larger teams on a batcher's small batches).  Other fields of
+ * *params (precision, entry mode, max_iter, hashes) are kept. */
 rte_status rte_autotune(rte_index* idx, const float* queries, int64_t nq, const int32_t* gt,
                         int gt_k, int k, float target_recall, rte_search_params* params,
                         rte_autotune_report* report);

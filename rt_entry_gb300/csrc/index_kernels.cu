@@ -752,18 +752,26 @@ cudaError_t launch_locate_dyn(const WideNode* wide, int n_wide, const float* pts
 // leave few collisions for batches of up to a few hundred thousand queries.
 constexpr int kOrderBins = 4096;
 constexpr int kOrderThreads = 1024;
-constexpr int kOrderKeys = 16;
+constexpr int kOrderKeys = 8;
 
-__device__ __forceinline__ int order_bin(int32_t leaf, int n_leaves) {
+// A range of 2^shift consecutive leaves per counter (shift: the smallest
+// that maps the last leaf below kOrderBins).
+__device__ __forceinline__ int order_bin(int32_t leaf, int n_leaves, int shift) {
   if (leaf < 0 || leaf >= n_leaves) leaf = 0;
-  return (int)(((int64_t)leaf * kOrderBins) / n_leaves);
+  return leaf >> shift;
 }
 
 __global__ void __launch_bounds__(kOrderThreads) order_by_leaf_kernel(const int32_t* __restrict__ leaf,
                                                                       int stride, int64_t n, int n_leaves,
-                                                                      int32_t* __restrict__ order) {
+                                                                      int shift, int32_t* __restrict__ order,
+                                                                      const int* n_dev, int64_t min_n) {
   __shared__ int cnt[kOrderBins];
   __shared__ int wsum[kOrderThreads / 32];
+  if (n_dev) {  // the live count, at most the capacity n
+    const int64_t live = *n_dev;
+    n = live < 0 ? 0 : live < n ? live : n;
+  }
+  if (n <= min_n) return;  // the whole block returns: n is uniform
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int i = tid; i < kOrderBins; i += kOrderThreads) cnt[i] = 0;
   __syncthreads();
@@ -775,7 +783,7 @@ __global__ void __launch_bounds__(kOrderThreads) order_by_leaf_kernel(const int3
 #pragma unroll
     for (int j = 0; j < kOrderKeys; ++j) {
       const int64_t q = r0 + (int64_t)j * kOrderThreads + tid;
-      b[j] = q < n ? order_bin(leaf[q * stride], n_leaves) : -1;
+      b[j] = q < n ? order_bin(leaf[q * stride], n_leaves, shift) : -1;
     }
 #pragma unroll
     for (int j = 0; j < kOrderKeys; ++j)
@@ -822,7 +830,7 @@ __global__ void __launch_bounds__(kOrderThreads) order_by_leaf_kernel(const int3
 #pragma unroll
     for (int j = 0; j < kOrderKeys; ++j) {
       const int64_t q = r0 + (int64_t)j * kOrderThreads + tid;
-      b[j] = q < n ? order_bin(leaf[q * stride], n_leaves) : -1;
+      b[j] = q < n ? order_bin(leaf[q * stride], n_leaves, shift) : -1;
     }
 #pragma unroll
     for (int j = 0; j < kOrderKeys; ++j)
@@ -831,10 +839,12 @@ __global__ void __launch_bounds__(kOrderThreads) order_by_leaf_kernel(const int3
 }
 
 cudaError_t launch_order_by_leaf(const int32_t* leaf, int stride, int64_t n, int n_leaves,
-                                 int32_t* order, cudaStream_t st) {
+                                 int32_t* order, cudaStream_t st, const int* n_dev, int64_t min_n) {
   if (n <= 0) return cudaSuccess;
   if (n > INT32_MAX || n_leaves < 1 || stride < 1) return cudaErrorInvalidValue;
-  order_by_leaf_kernel<<<1, kOrderThreads, 0, st>>>(leaf, stride, n, n_leaves, order);
+  int shift = 0;
+  while (((n_leaves - 1) >> shift) >= kOrderBins) ++shift;
+  order_by_leaf_kernel<<<1, kOrderThreads, 0, st>>>(leaf, stride, n, n_leaves, shift, order, n_dev, min_n);
   return cudaGetLastError();
 }
 

@@ -126,9 +126,14 @@ cudaError_t launch_locate(const WideNode* wide, int n_wide, const float* pts, in
 // numbered in the kd-tree build's depth-first order, so queries close in
 // the order start in nearby parts of the base, and the queries a persistent
 // search runs at the same time then share more graph rows and vectors in
-// L2.  Within one of the 4096 leaf ranges the order is that of the atomic
-// counters; each query's result does not depend on it.  One block.
+// L2.  Within one of the (at most 4096) ranges of 2^s consecutive leaves
+// the order is that of the atomic counters; each query's result does not
+// depend on it.  One block.
+// For graph replay, n_dev gives the live count (n is then the capacity),
+// and a live count of min_n or fewer writes nothing: the search reads the
+// order only for more than min_n queries (SearchArgs::order_min).
 cudaError_t launch_order_by_leaf(const int32_t* leaf, int stride, int64_t n, int n_leaves,
-                                 int32_t* order, cudaStream_t st);
+                                 int32_t* order, cudaStream_t st, const int* n_dev = nullptr,
+                                 int64_t min_n = 0);
 
 }  // namespace rte

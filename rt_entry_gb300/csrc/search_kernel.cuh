@@ -1439,11 +1439,12 @@ __host__ __device__ constexpr int search_min_blocks(int C, int NL, int NB) {
 }
 
 // The next query of the persistent loop (one lane): the work counter's
-// next slot, through the order permutation when there is one; nq or more
-// once every query is taken.
+// next slot, through the order permutation when there is one (written for
+// batches of more than a.order_min queries); nq or more once every query
+// is taken.
 __device__ __forceinline__ int next_query(const SearchArgs& a, int nq) {
   const int t = (int)atomicAdd(a.work, 1u);
-  return a.order && t < nq ? __ldg(a.order + t) : t;
+  return a.order && nq > a.order_min && t < nq ? __ldg(a.order + t) : t;
 }
 
 template <int C, int NL, int NB, int PREC, bool R16 = false>

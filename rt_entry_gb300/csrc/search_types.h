@@ -63,6 +63,7 @@ struct SearchArgs {
                             // by the kernel from the live query count, at least -team
   int* err;                 // device word set to a non-zero code when a bounded wait runs out, or null
   const int32_t* order;     // [nq] the order in which queries are taken (a permutation), or null
+  int order_min;            // the order is read only for more than this many queries
 };
 
 }  // namespace rte

@@ -80,6 +80,27 @@ def test_learned_batcher_equals_direct_search(lib, cuda):
         b.close()
 
 
+def test_batchers_take_large_batches_in_leaf_order(lib, cuda):
+    """A live batch of more queries than the resident warps (at most 4,864 on
+    152 SMs) runs the graph's sort kernel and takes its queries in entry-leaf
+    order, by the kd-tree leaf or, with learned entries, by the kd-tree leaf
+    computed beside the model; a small batch through the same graph skips
+    the order.  Every batch equals the direct search, which orders large
+    batches the same way and is checked against the oracle."""
+    import rt_entry_gb300 as r
+    from rt_entry_gb300 import datasets as ds
+    idx, base, q = _index(nq=12000, seed=47)
+    idx.train_learned(ds.mixture_config(2).sample(20000, 79))
+    for mode in (r.ENTRY_KDTREE, r.ENTRY_LEARNED):
+        p = r.default_params(beam=16, k=10, precision=r.PREC_BF16, rerank=1, entry_mode=mode)
+        b = idx.batcher(12000, params=p)
+        for s, e in [(0, 12000), (0, 50), (50, 9050)]:
+            want, wd = idx.search(q[s:e], params=p)
+            ids, dd = b.search(q[s:e])
+            assert np.array_equal(ids, want) and np.array_equal(dd, wd), (mode, s, e)
+        b.close()
+
+
 def test_autotune_meets_the_recall_target(lib, cuda):
     import rt_entry_gb300 as r
     from rt_entry_gb300 import datasets as ds
