@@ -884,8 +884,9 @@ def main():
                        "h2d_bytes_per_step": int(nq * d * 4),
                        "d2h_bytes_per_step": int(nq * K_TOP * 8)},
                # per timed step of the headline arm: project_tf32_kernel, locate_points
-               # (side stream), mlp_head_kernel, locate_in_subtree_wide, search_kernel
-               "gpu_launches": 5 * args.steps,
+               # and order_by_leaf_kernel (side stream), mlp_head_kernel,
+               # locate_in_subtree_wide, search_kernel
+               "gpu_launches": 6 * args.steps,
                "clocks": clocks}
         det = json.dumps(B.details)
         print(f"[bench-details] {det}", file=sys.stderr, flush=True)
