@@ -141,7 +141,9 @@ rte_status rte_locate(rte_index* idx, const float* projected, int64_t nq, int32_
  * RTE_ETIMEOUT if a bounded device wait in the path ran out (the learned
  * head's pipeline, or a search warp waiting on the block's tail helpers);
  * with device buffers the call is asynchronous and such a wait only sets
- * a device word.  The same holds for rte_search_projected. */
+ * a device word.  Page-locked host outputs are written by the kernels
+ * directly; pageable ones are filled by copies after the search.  The same
+ * holds for rte_search_projected. */
 rte_status rte_search(rte_index* idx, const float* queries, int64_t nq,
                       const rte_search_params* params, int32_t* out_ids, float* out_dists,
                       void* stream);

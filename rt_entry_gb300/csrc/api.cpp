@@ -75,6 +75,16 @@ bool is_device_ptr(const void* p) {
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
+// The device address of page-locked host memory that the device can reach
+// (every page-locked allocation under unified addressing), else null.
+void* mapped_host_ptr(void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
 rte_status noalloc_prepare(int dev);
 namespace tc {
 void set_wait_limit(long long rounds);  // tc_common.cuh
@@ -928,15 +938,25 @@ static rte_status search_common(rte_index* x, const float* q, bool projected, co
     RTE_CUDA(cudaMemcpyAsync(hb.p, hits, hbytes, cudaMemcpyHostToDevice, st));
     dh = hb.as<int32_t>();
   }
+  // Page-locked host outputs are written by the kernels themselves, through
+  // their device address: each query's results cross the host link as the
+  // query finishes, overlapped with the rest of the search, instead of in
+  // copies after it.  Pageable host outputs go through device buffers.
   int32_t* di = out_ids;
   const bool ids_host = out_ids && !is_device_ptr(out_ids);
-  if (!out_ids || ids_host) {
+  int32_t* ids_mapped = ids_host ? static_cast<int32_t*>(mapped_host_ptr(out_ids)) : nullptr;
+  if (ids_mapped) {
+    di = ids_mapped;
+  } else if (!out_ids || ids_host) {
     RTE_CUDA(ib.alloc(obytes, st));
     di = ib.as<int32_t>();
   }
   float* dd = out_dists;
   const bool dists_host = out_dists && !is_device_ptr(out_dists);
-  if (dists_host) {
+  float* dists_mapped = dists_host ? static_cast<float*>(mapped_host_ptr(out_dists)) : nullptr;
+  if (dists_mapped) {
+    dd = dists_mapped;
+  } else if (dists_host) {
     RTE_CUDA(db.alloc(obytes, st));
     dd = db.as<float>();
   }
@@ -957,8 +977,9 @@ static rte_status search_common(rte_index* x, const float* q, bool projected, co
   if (syncs) *herr = 0;
   s = run_query_path(x, dq, projected, dh, nq, prm, di, dd, dc, st, syncs ? herr : nullptr);
   if (s != RTE_OK) return s;
-  if (ids_host) RTE_CUDA(cudaMemcpyAsync(out_ids, di, obytes, cudaMemcpyDeviceToHost, st));
-  if (dists_host) RTE_CUDA(cudaMemcpyAsync(out_dists, dd, obytes, cudaMemcpyDeviceToHost, st));
+  if (ids_host && !ids_mapped) RTE_CUDA(cudaMemcpyAsync(out_ids, di, obytes, cudaMemcpyDeviceToHost, st));
+  if (dists_host && !dists_mapped)
+    RTE_CUDA(cudaMemcpyAsync(out_dists, dd, obytes, cudaMemcpyDeviceToHost, st));
   if (cnt_host) RTE_CUDA(cudaMemcpyAsync(counters, dc, (size_t)nq * 32, cudaMemcpyDeviceToHost, st));
   if (syncs) {
     RTE_CUDA(cudaStreamSynchronize(st));

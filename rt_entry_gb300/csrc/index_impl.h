@@ -19,6 +19,7 @@ rte_status fail(rte_status s, const std::string& msg);
 rte_status ensure_precision(rte_index* x, int precision);
 void clear_error();
 bool is_device_ptr(const void* p);
+void* mapped_host_ptr(void* p);
 // Launch plan of a search of nq queries (api.cpp): pool and batch shape,
 // warps per block, grid, shared memory and warps per query; *ordered is
 // set when the batch outnumbers the resident warps and has entry leaves, so

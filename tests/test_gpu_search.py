@@ -294,6 +294,19 @@ def test_topk_prefix_and_host_device_io(lib, orc, cuda):
     it2, _ = idx.search_projected(qt, beam=64, k=10, stream=s)
     s.synchronize()
     assert np.array_equal(it2.cpu().numpy(), top)
+    # host queries and outputs: pageable outputs come back by copy,
+    # page-locked ones are written by the kernels through their device address
+    hi, hd = idx.search(q, beam=64, k=10)
+    assert np.array_equal(hi, top) and np.array_equal(hd, td)
+    pi = torch.full((q.shape[0], 10), -7, dtype=torch.int32).pin_memory()
+    pd = torch.full((q.shape[0], 10), float("nan"), dtype=torch.float32).pin_memory()
+    idx.search(torch.from_numpy(q).pin_memory(), beam=64, k=10, out_ids=pi, out_dists=pd, stream=s)
+    assert np.array_equal(pi.numpy(), top) and np.array_equal(pd.numpy(), td)
+    # only the ids page-locked, the distances pageable
+    pi.fill_(-7)
+    nd = np.full((q.shape[0], 10), np.nan, np.float32)
+    idx.search(q, beam=64, k=10, out_ids=pi, out_dists=nd)
+    assert np.array_equal(pi.numpy(), top) and np.array_equal(nd, td)
 
 
 def test_pca_against_fp64_and_reference_golden(lib, cuda):
