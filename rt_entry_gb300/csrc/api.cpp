@@ -220,8 +220,10 @@ namespace rte {
 // The fewest warps per query that automatic teams use.  FP32 rows with pools
 // of up to 64 slots: their gathers bound the search, and two warps per query
 // keep twice the rows in flight, which is faster even when the batch fills
-// the GPU (measured on one GB300 at 10k and 40k queries: 9-17 % at beams
-// 16 to 64; no gain at 128 and 256, nor for BF16 or FP8 rows).
+// the GPU a few times over (measured on one GB300 with queries in leaf
+// order: 6-11 % at 10k queries, beams 16 to 64).  Above kTeamFloorLoad
+// times the resident warps one warp per query wins (9-20 % at 40k queries),
+// as it always does at beams 128 and 256 and for BF16 or FP8 rows.
 int team_floor(int prec, int L, int wpb) {
   return prec == kPrecF32 && L <= 64 && wpb % 2 == 0 ? 2 : 1;
 }
@@ -295,6 +297,7 @@ rte_status plan_search(const rte_index* x, const rte_search_params* prm, int64_t
   pl.team = team;
   if (team == 0) {  // automatic: spread a small batch's queries over the idle warps
     pl.team = team_floor(pl.prec, pl.L, pl.wpb);
+    if (nq > kTeamFloorLoad * resident) pl.team = 1;
     while (pl.team < 8 && pl.wpb % (2 * pl.team) == 0 && nq * 2 * pl.team <= resident) pl.team *= 2;
   }
   const int64_t need = (nq * pl.team + pl.wpb - 1) / pl.wpb;

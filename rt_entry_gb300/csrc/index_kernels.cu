@@ -775,8 +775,8 @@ __global__ void __launch_bounds__(kOrderThreads) order_by_leaf_kernel(const int3
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int i = tid; i < kOrderBins; i += kOrderThreads) cnt[i] = 0;
   __syncthreads();
-  // each thread issues kOrderKeys independent loads per round, so that a
-  // batch of up to kOrderKeys * 1024 queries costs one memory latency per
+  // each thread issues kOrderKeys independent loads per loop trip, so that
+  // a batch of up to kOrderKeys * 1024 queries costs one memory latency per
   // pass rather than a chain of them
   for (int64_t r0 = 0; r0 < n; r0 += (int64_t)kOrderKeys * kOrderThreads) {
     int b[kOrderKeys];

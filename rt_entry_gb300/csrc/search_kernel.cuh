@@ -1486,8 +1486,9 @@ __global__ void __launch_bounds__(256, search_min_blocks(C, NL, NB)) search_kern
 }
 
 // search_kernel with teams of K warps per query (Team): K = a.team, or,
-// for a.team < 0, at least -a.team and otherwise the most (up to 8) that the
-// live query count leaves room for in the grid.  K = 1 runs as a team of one.  A kernel of its own, so
+// for a.team < 0, at least -a.team (one above kTeamFloorLoad times the
+// grid's warps) and otherwise the most (up to 8) that the live query count
+// leaves room for in the grid.  K = 1 runs as a team of one.  A kernel of its own, so
 // that the single-warp kernel's code and register allocation stay as they
 // are; a team never spans blocks (the launch keeps warps per block a
 // multiple of K, and K falls back to 1 otherwise).
@@ -1516,6 +1517,7 @@ __global__ void __launch_bounds__(256, search_min_blocks(C, NL, NB)) search_kern
   if (K < 0) {  // at least -a.team warps, then as many as the live batch leaves room for
     const long long total = (long long)gridDim.x * wpb;
     K = -a.team;
+    if ((long long)nq > kTeamFloorLoad * total) K = 1;  // the floor holds for moderate batches only
     while (K < 8 && wpb % (2 * K) == 0 && (long long)nq * 2 * K <= total) K *= 2;
   }
   if (K < 1 || K > 8 || wpb % K != 0) K = 1;

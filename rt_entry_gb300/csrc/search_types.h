@@ -29,6 +29,10 @@ RTE_HD constexpr int query_slot_words_for(int C, int chunks) {
 // (a power of two >= 32 words), the compaction words (2 x 16..256) and the
 // query slot (64 or 32 x chunks words) are all multiples of 4 words.
 constexpr int kTeamCtlWords = 4;
+// Automatic teams keep their floor of warps per query (more than one: FP32
+// rows with pools of up to 64 slots) only while a batch is at most this
+// many times the resident warps; above it one warp per query is faster.
+constexpr int kTeamFloorLoad = 3;
 // Shared memory a search block keeps after its warps' regions: the tail
 // helping state (a count of idle warps and one phase descriptor per warp,
 // search_kernel.cuh's BlockShare).  Every launch reserves it.

@@ -80,6 +80,24 @@ def test_learned_batcher_equals_direct_search(lib, cuda):
         b.close()
 
 
+def test_large_batches_drop_the_two_warp_floor(lib, cuda):
+    """FP32 rows with small pools get two warps per query only while a batch
+    is at most three times the resident warps (4,864 on 152 SMs): 16,000
+    queries run one warp per query, chosen on the host by rte_search and on
+    the device by the batcher's graph, with the results of one warp per
+    query; a 4,000-query batch through the same graph keeps the floor."""
+    import rt_entry_gb300 as r
+    idx, base, q = _index(nq=16000, seed=49)
+    want, wd = idx.search(q, params=r.default_params(beam=16, k=10, team_warps=1))
+    got, gd = idx.search(q, params=r.default_params(beam=16, k=10))
+    assert np.array_equal(got, want) and np.array_equal(gd, wd)
+    b = idx.batcher(16000, params=r.default_params(beam=16, k=10))
+    for s, e in [(0, 16000), (0, 4000)]:
+        ids, dd = b.search(q[s:e])
+        assert np.array_equal(ids, want[s:e]) and np.array_equal(dd, wd[s:e]), (s, e)
+    b.close()
+
+
 def test_batchers_take_large_batches_in_leaf_order(lib, cuda):
     """A live batch of more queries than the resident warps (at most 4,864 on
     152 SMs) runs the graph's sort kernel and takes its queries in entry-leaf
