@@ -19,7 +19,10 @@
 //     using one shuffle per neighbour instead of five;
 //   * the visited-set bloom filter lives in shared memory per warp, sized at
 //     run time (the reference fixes 512 words, graph_search.cuh:4-5);
-//   * warps pull queries from an atomic counter until none are left.
+//   * warps pull queries from an atomic counter until none are left; a
+//     batch larger than the resident warps is pulled through a permutation
+//     that groups its queries by entry leaf (SearchArgs::order), so that
+//     the queries running at the same time share rows in L2.
 #pragma once
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
