@@ -417,6 +417,14 @@ rte_status rte_knn_graph(const float* base, int64_t n, int d, int degree, int de
  * path.  (No reference counterpart.) */
 void rte_set_wait_limit(long long rounds);
 
+/* The library's scratch memory pool on `device` (the stream-ordered pool
+ * the query calls take their per-call buffers from; it keeps up to 1 GiB
+ * mapped between calls): bytes in use now and the high-water mark (either
+ * pointer may be NULL), then, if reset_high, the mark restarts from the
+ * current use.  For monitoring, and for tests that a call allocates
+ * nothing.  (No reference counterpart.) */
+rte_status rte_scratch_pool_usage(int device, uint64_t* used_now, uint64_t* used_high, int reset_high);
+
 /* Message of the last failure on this thread ("" if none). */
 const char* rte_last_error(void);
 

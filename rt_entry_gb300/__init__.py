@@ -34,7 +34,7 @@ EXPORTS = (
     "rte_default_train_params", "rte_learned_train", "rte_learned_predict", "rte_mlp_grad_check",
     "rte_search_projected_noalloc", "rte_gemm_bf16_bias_argmax", "rte_mlp_head_argmax", "rte_knn_graph", "rte_locate_multi", "rte_batcher_create", "rte_batcher_search", "rte_batcher_k",
     "rte_batcher_free", "rte_autotune", "rte_set_wait_limit", "rte_index_load_reference",
-    "rte_read_vectors", "rte_index_prepare", "rte_index_release",
+    "rte_read_vectors", "rte_index_prepare", "rte_index_release", "rte_scratch_pool_usage",
 )
 
 

@@ -1,9 +1,10 @@
 // api.cpp -- C ABI of rt_entry_gb300 (include/rtentry.h).
 //
 // The index object owns every device buffer of one index on one GPU.  Query
-// calls allocate their per-call buffers from the device's stream-ordered
-// memory pool (cudaMallocAsync on the caller's stream), so calls on distinct
-// streams do not share scratch and the pool keeps memory warm across calls.
+// calls allocate their per-call buffers from the library's stream-ordered
+// memory pool on that device (scratch_pool, on the caller's stream), so
+// calls on distinct streams do not share scratch and the pool keeps memory
+// mapped across calls and synchronisations.
 #include "rtentry.h"
 
 #include <cuda_runtime.h>
@@ -75,6 +76,37 @@ bool is_device_ptr(const void* p) {
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
+cudaMemPool_t scratch_pool() {
+  constexpr int kMaxDevices = 64;
+  static std::mutex mu;
+  static cudaMemPool_t pools[kMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (!pools[dev]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    if (cudaMemPoolCreate(&p, &props) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    unsigned long long keep = kScratchKeepBytes;
+    if (cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+      cudaGetLastError();
+      cudaMemPoolDestroy(p);
+      return nullptr;
+    }
+    pools[dev] = p;
+  }
+  return pools[dev];
+}
+
 // The device address of page-locked host memory that the device can reach
 // (every page-locked allocation under unified addressing), else null.
 void* mapped_host_ptr(void* p) {
@@ -559,6 +591,33 @@ void rte_default_params(rte_search_params* p) {
 const char* rte_last_error(void) { return g_err.c_str(); }
 
 void rte_set_wait_limit(long long rounds) { rte::tc::set_wait_limit(rounds); }
+
+rte_status rte_scratch_pool_usage(int device, uint64_t* used_now, uint64_t* used_high, int reset_high) {
+  g_err.clear();
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(RTE_ECUDA, "cudaGetDeviceCount failed");
+  }
+  if (device < 0 || device >= n) return fail(RTE_EINVAL, "device index out of range");
+  DeviceGuard g(device);
+  cudaMemPool_t pool = scratch_pool();
+  if (!pool) return fail(RTE_ECUDA, "the scratch memory pool could not be created");
+  unsigned long long v = 0;
+  if (used_now) {
+    RTE_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &v));
+    *used_now = v;
+  }
+  if (used_high) {
+    RTE_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &v));
+    *used_high = v;
+  }
+  if (reset_high) {
+    unsigned long long zero = 0;
+    RTE_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero));
+  }
+  return RTE_OK;
+}
 
 rte_status rte_index_from_host(const float* base, int64_t np, int dim, const int32_t* graph,
                                int degree, int device, rte_index** out) {

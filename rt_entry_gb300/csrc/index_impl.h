@@ -76,6 +76,16 @@ struct DevBuf {
 
 // Device scratch from the stream-ordered pool, released on scope exit
 // (stream-ordered, so the memory is reused only after prior work finishes).
+// The library's stream-ordered memory pool on the current device (created
+// on first use, kept until the process exits), or null if it cannot be
+// made.  It keeps up to kScratchKeepBytes mapped across synchronisations,
+// so that a call after a synchronising call does not map its scratch again;
+// the device's default pool, which releases everything at each
+// synchronisation unless its owner says otherwise, is left to the host
+// program.
+constexpr unsigned long long kScratchKeepBytes = 1ull << 30;
+cudaMemPool_t scratch_pool();
+
 struct AsyncBuf {
   void* p = nullptr;
   cudaStream_t st = nullptr;
@@ -87,7 +97,9 @@ struct AsyncBuf {
   cudaError_t alloc(size_t bytes, cudaStream_t s) {
     st = s;
     if (bytes == 0) bytes = 16;
-    return cudaMallocAsync(&p, bytes, s);
+    cudaMemPool_t pool = scratch_pool();
+    if (!pool) return cudaErrorMemoryAllocation;
+    return cudaMallocFromPoolAsync(&p, bytes, pool, s);
   }
   template <typename T>
   T* as() const {

@@ -6,9 +6,9 @@ allocator that owns the device).  Its output must equal the allocating entry
 point's -- ids and distances bit for bit, the bar of every search test here --
 on two calls in a row, since the second call reuses the scratch array the
 first one left behind.  The second call must also allocate nothing: the
-device's default memory pool (which the library's other entry points draw
-their scratch from) records no use, and the free device memory does not
-move.  The file sorts last so that a run stopping at the first failure has
+library's scratch pool (which its other entry points draw their per-call
+buffers from) and the device's default pool record no use, and the free
+device memory does not move.  The file sorts last so that a run stopping at the first failure has
 already run every other test.
 """
 import ctypes
@@ -20,6 +20,31 @@ pytestmark = pytest.mark.gpu
 
 _CU_MEMPOOL_ATTR_USED_MEM_CURRENT = 7  # CUmemPool_attribute, cuda.h
 _CU_MEMPOOL_ATTR_USED_MEM_HIGH = 8
+
+
+class _ScratchPool:
+    """The library's own stream-ordered pool on one device, through
+    rte_scratch_pool_usage."""
+
+    def __init__(self, lib, ordinal=0):
+        self.lib, self.dev = lib, ordinal
+        lib.rte_scratch_pool_usage.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_uint64),
+                                               ctypes.POINTER(ctypes.c_uint64), ctypes.c_int]
+        lib.rte_scratch_pool_usage.restype = ctypes.c_int
+
+    def _get(self, reset=0):
+        now, high = ctypes.c_uint64(), ctypes.c_uint64()
+        assert self.lib.rte_scratch_pool_usage(self.dev, ctypes.byref(now), ctypes.byref(high), reset) == 0
+        return now.value, high.value
+
+    def reset_used_high(self):
+        self._get(reset=1)
+
+    def used_now(self):
+        return self._get()[0]
+
+    def used_high(self):
+        return self._get()[1]
 
 
 class _DefaultPool:
@@ -82,6 +107,7 @@ def test_noalloc_search_equals_allocating_search(lib, cuda):
     nq = qp.shape[0]
     leaves = idx.locate(qp)  # caller-supplied entry leaves (device memory)
     pool = _DefaultPool(torch.cuda.current_device())
+    scratch = _ScratchPool(lib, torch.cuda.current_device())
     for kw, hits in ((dict(beam=64, k=10), None),
                      (dict(beam=128, k=128, precision=r.PREC_BF16, rerank=1), None),
                      (dict(beam=32, k=16, entry_mode=r.ENTRY_RANDOM), None),
@@ -100,12 +126,15 @@ def test_noalloc_search_equals_allocating_search(lib, cuda):
                 free0 = torch.cuda.mem_get_info()[0]
                 used0 = pool.used_now()
                 pool.reset_used_high()
+                sused0 = scratch.used_now()
+                scratch.reset_used_high()
             rc, ids, dd = _noalloc(lib, idx, qp, hits, params, nq, ids, dd)
             assert rc == r.RTE_OK, lib.rte_last_error()
             assert torch.equal(ids, want_ids), (kw, call)
             assert torch.equal(dd, want_d), (kw, call)
             if call == 1:
                 assert pool.used_high() <= used0, "the call drew memory from the default pool"
+                assert scratch.used_high() <= sused0, "the call drew memory from the scratch pool"
                 assert torch.cuda.mem_get_info()[0] == free0, "the call changed the free device memory"
 
 
