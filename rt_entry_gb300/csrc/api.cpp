@@ -207,12 +207,10 @@ rte_status create_index(const float* base, int64_t np, int dim, const int32_t* g
   x->np = np;
   x->dim = dim;
   x->degree = degree;
-  // stream-ordered pool keeps freed scratch for reuse
-  cudaMemPool_t pool;
-  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
-    uint64_t thr = UINT64_MAX;
-    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-  }
+  // the library's scratch pool on this device, made here rather than in the
+  // first search (a new pool holds no memory); the device's default pool is
+  // the host program's and keeps its settings
+  scratch_pool();
   std::vector<int32_t> hg;
   const int32_t* gh = graph;
   if (gdev) {
